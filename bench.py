@@ -1,0 +1,314 @@
+"""Benchmark of the GB300 photon propagator.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+Workload (one "step"): the three-layer stack between n = 1.52 slides
+(n=1.37/1.40/1.44, mua=0.5/2.0/0.2 1/cm, mus=200/120/50 1/cm, g=0.8/0.9/0.75,
+d=0.01/0.15/0.3 cm; slides 0.1 cm), two 5.08 cm spheres with 1.27/1.27/0.635 cm
+ports and wall reflectance 0.98, crosstalk on, 1e8 photon packets, seed 7 --
+one full forward simulation.  Metric: photons/s.
+
+GPU arm (default): `value` is timed with CUDA events around the device-pointer
+entry point (instances already in HBM); `e2e` times the host-pointer C ABI call
+(ismc_run_batch: H2D of the instance, prepare, scan, propagate, D2H of the
+tally) with a host clock.  L2 is flushed (a 512 MB write) before every timed
+step.  Under torchrun each rank simulates its own packet range of the same
+stack (weak scaling) and the max time over ranks is reported.
+
+Reference arm (--impl reference): the reference's algorithm on the host cores,
+as restated in FP64 C from ISMLMC.py / MLMC.py (oracle/ismc_ref64.c: the
+reference itself is Python and cannot run on the GPU machine), each step a
+bounded packet sample of the same workload.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PACKETS = 100_000_000
+SEED = 7
+L2_FLUSH_BYTES = 512 << 20
+ROOFLINE_FILE = os.path.join(ROOT, "profiles", "propagator_bench1_roofline.json")
+
+
+def workload_layers():
+    from ismc_gb300 import Layer
+    return [Layer.slide(1.52, 0.1), Layer(1.37, 0.5, 200.0, 0.8, 0.01),
+            Layer(1.40, 2.0, 120.0, 0.9, 0.15), Layer(1.44, 0.2, 50.0, 0.75, 0.3),
+            Layer.slide(1.52, 0.1)]
+
+
+def workload_spheres():
+    from ismc_gb300 import Spheres
+    return Spheres.from_radii(5.08, 1.27, 1.27, 0.635, 0.98, R=True, T=True)
+
+
+def workload_instance(n, offset=0):
+    from ismc_gb300 import make_instance
+    return make_instance(workload_layers(), workload_spheres(), n, seed=SEED, mode="compat",
+                         roulette_threshold=1e-4, roulette_m=10.0, packet_offset=offset)
+
+
+CONFIG = {"workload": "3-layer stack between n=1.52 slides, two 5.08 cm spheres with crosstalk, "
+                      "1e8 packets per step (configs[1] of the benchmark set)",
+          "layers": 5, "packets_per_step": PACKETS, "seed": SEED, "mode": "compat",
+          "l2": "flushed (512 MB write) before every timed step"}
+
+
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index),
+                                          f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace('.', '', 1).isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace('.', '', 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def cpu_baseline(seconds=12.0):
+    """The reference's algorithm (FP64 restatement of ISMLMC.py) on all host
+    cores, on a bounded packet sample of the workload."""
+    import oracle
+    threads = os.cpu_count()
+    n = 20000
+    t0 = time.perf_counter()
+    oracle.ref64_run(workload_instance(n), threads=threads)
+    dt = time.perf_counter() - t0
+    n2 = max(n, int(n * seconds / max(dt, 1e-3)))
+    t0 = time.perf_counter()
+    _, _, steps = oracle.ref64_run(workload_instance(n2), threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n2 / dt, "unit": "photons/s", "cores": threads, "kind": "port",
+            "sample": f"{n2} packets of the workload (FP64 C restatement of ISMLMC.py/MLMC.py, "
+                      f"{threads} threads, {dt:.1f} s)", "steps_per_s": steps / dt}
+
+
+def load_roofline_profile():
+    try:
+        with open(ROOFLINE_FILE) as fh:
+            return json.load(fh)
+    except Exception:
+        return None
+
+
+# ----------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import oracle
+    oracle.lib()
+    threads = os.cpu_count()
+    # size one step to ~10 s of host work
+    n = 20000
+    t0 = time.perf_counter()
+    oracle.ref64_run(workload_instance(n), threads=threads)
+    dt = time.perf_counter() - t0
+    per_step = max(n, int(n * 10.0 / max(dt, 1e-3)))
+    for w in range(args.warmup):
+        oracle.ref64_run(workload_instance(min(per_step, 20000), offset=w * per_step),
+                         threads=threads)
+    times = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.ref64_run(workload_instance(per_step, offset=k * per_step), threads=threads)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = per_step * args.steps / total
+    line = {"metric": "photons/s", "value": value, "unit": "photons/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": dict(CONFIG, packets_per_step=per_step,
+                           note="each step is a bounded packet sample of the workload"),
+            "cpu_baseline": {"value": value, "unit": "photons/s", "cores": threads, "kind": "port",
+                             "sample": f"{per_step} packets per step, FP64 C restatement of "
+                                       f"ISMLMC.py/MLMC.py on {threads} threads"},
+            "e2e": {"value": value, "unit": "photons/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world, dist):
+    import torch
+    from ismc_gb300 import Engine, _abi, build
+    build.build()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    eng = Engine(dev)
+    n = args.packets
+    inst = workload_instance(n, offset=rank * n)
+    raw = bytes(inst)
+    d_in = torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(f"cuda:{dev}")
+    d_out = torch.zeros(C.sizeof(_abi.Tally), dtype=torch.uint8, device=f"cuda:{dev}")
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{dev}")
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def device_step():
+        eng.run_batch_device(d_in.data_ptr(), 1, d_out.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        device_step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timing (CUDA events on the launching stream)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            ev[k][0].record(stream)
+            device_step()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    dev_time = sum(ms) / 1000.0
+    tally = (_abi.Tally).from_buffer_copy(d_out.cpu().numpy().tobytes())
+    if tally.status != 0:
+        raise RuntimeError(f"propagator status {tally.status}")
+
+    # ---- end-to-end through the host-pointer C ABI (ismc_run_batch)
+    e2e_times = []
+    res = None
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        res = eng.run_batch([inst])[0]
+        e2e_times.append(time.perf_counter() - t0)
+    barrier()
+    e2e_time = sum(e2e_times)
+
+    if dist is not None:
+        t = torch.tensor([dev_time, e2e_time], dtype=torch.float64, device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_time, e2e_time = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+    total_packets = n * args.steps * world
+    value = total_packets / dev_time
+    e2e = total_packets / e2e_time
+    steps_per_packet = tally.steps / n
+    events_per_packet = tally.events / n
+    clocks = clk.summary()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    prof = load_roofline_profile()
+    roof = {"bound": "issue", "unit": "Gthread-inst/s", "achieved": None, "peak": None,
+            "frac": None, "traffic": None,
+            "note": "issue-rate roofline: SMs x SM clock x 128 lanes vs photon-steps/s x "
+                    "thread-instructions per step (ncu, profiles/)"}
+    steps_per_s = tally.steps * world * args.steps / dev_time
+    if prof and clocks.get("sm_mhz"):
+        ips = float(prof["thread_inst_per_step"])
+        peak = sms * clocks["sm_mhz"] * 1e6 * 128 / 1e9
+        ach = steps_per_s * ips / 1e9
+        roof.update(achieved=ach, peak=peak, frac=ach / peak,
+                    traffic=prof.get("dram_bytes_per_launch"),
+                    thread_inst_per_step=ips, steps_per_s=steps_per_s,
+                    roofline_steps_per_s=peak * 1e9 / ips, clock="median SM clock under load",
+                    source=os.path.relpath(ROOFLINE_FILE, ROOT))
+    else:
+        roof.update(steps_per_s=steps_per_s)
+    cpu = cpu_baseline() if (world == 1 and not args.no_cpu_baseline) else None
+    line = {"metric": "photons/s", "value": value, "unit": "photons/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dev_time / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": CONFIG,
+            "e2e": {"value": e2e, "unit": "photons/s", "h2d_bytes_per_step": C.sizeof(_abi.Instance),
+                    "d2h_bytes_per_step": C.sizeof(_abi.Tally),
+                    "api": "ismc_run_batch (host pointers)"},
+            "gpu_launches": 3 * args.steps,
+            "clocks": clocks,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "result": {"R_d": res.mean[1], "T_d": res.mean[3], "T_u": res.mean[4],
+                       "se": [res.se[1], res.se[3], res.se[4]],
+                       "steps_per_packet": steps_per_packet, "events_per_packet": events_per_packet}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--packets", type=int, default=PACKETS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        tdist.init_process_group(backend)
+        dist = tdist
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_gpu(args, rank, world, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,193 @@
+/*
+ * ismc.h -- C ABI of the GB300 integrating-sphere Monte Carlo propagator.
+ *
+ * This is the boundary the reference's forward model is replaced behind.  The
+ * reference exposes its forward model three ways, all of which map onto the
+ * entry points below:
+ *
+ *   ISMC.py:164-406      ISMC(N, n, g, t, mu_a, mu_s, mu_t, R, R_pw, ..., T_angle)
+ *                        -> (A, R_d, R_s, T_d, T_u) as fractions of N  (one slab)
+ *   ISMLMC.py:101-347    ISMLMC(...) with list-valued n/g/t/mu_a/mu_s/mu_t (stack)
+ *   CUDA/CUDAISMLMC.h:656-755
+ *                        thrust::tuple<float x5> ISMLMC(int dev, int N, int layers,
+ *                        float* n, float* g, float* t, float* bounds, float* mu_a,
+ *                        float* mu_s, float* mu_t, bool R, float R_pw, ...)
+ *
+ * Conventions
+ *   - Plain C, fixed-width types, natural alignment, no packing pragmas: every
+ *     struct below has explicit padding so its layout is the same for C, C++,
+ *     ctypes and any other FFI.
+ *   - Every entry point returns 0 on success or a negative ISMC_ERR_* code.
+ *     Nothing calls exit() (contrast CUDA/CUDAISMLMC.h:41-48).  The text of the
+ *     last error of a context is available from ismc_last_error().
+ *   - Caller owns every host array it passes; nothing is retained after return.
+ *   - A context owns its device buffers, stream and graphs.  One context must
+ *     not be used from two threads at once without an external lock; separate
+ *     contexts are independent (no global mutable state in the library).
+ *   - Results are integer fixed-point sums (scale 2^-scale_log2 per unit of
+ *     packet weight), so a given (seed, stream, packet range) is bit-identical
+ *     for any launch shape, chunking or sharding.
+ */
+#ifndef ISMC_GB300_H
+#define ISMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ISMC_ABI_VERSION 1
+#define ISMC_MAXL 16            /* max layers in a stack (slides count as layers) */
+
+/* error codes */
+#define ISMC_OK 0
+#define ISMC_ERR_INVALID_ARG   (-1)
+#define ISMC_ERR_CUDA          (-2)
+#define ISMC_ERR_STEP_LIMIT    (-3)   /* some packet exceeded the per-packet event cap */
+#define ISMC_ERR_NO_DEVICE     (-4)
+#define ISMC_ERR_ALLOC         (-5)
+#define ISMC_ERR_CAPACITY      (-6)   /* request larger than a fixed-capacity buffer */
+#define ISMC_ERR_INTERNAL      (-7)
+
+/* propagation modes */
+#define ISMC_MODE_COMPAT   0u   /* reproduce ISMC.py / ISMLMC.py+MLMC.MC semantics */
+#define ISMC_MODE_PHYSICAL 1u   /* physically consistent slides / re-incidence */
+
+/* tally order (index into ismc_tally.sum / sumsq) -- the reference's return order */
+#define ISMC_T_A   0
+#define ISMC_T_RD  1
+#define ISMC_T_RS  2
+#define ISMC_T_TD  3
+#define ISMC_T_TU  4
+
+/*
+ * A layer stack, top (index 0, facing the R sphere) to bottom.  A layer with
+ * mus == 0 is a non-scattering slide ("glass"), as in ISMLMC.py:81 and
+ * MLMC.py:97.  mut is the interaction coefficient the walk uses
+ * (the reference's callers pass mu_a + mu_s: lookup.py:238, minimization.py:205).
+ * Units: 1/cm and cm.  The ambient index is 1 on both sides.
+ */
+typedef struct ismc_stack {
+    uint32_t L;
+    uint32_t _pad0;
+    float n[ISMC_MAXL];
+    float mua[ISMC_MAXL];
+    float mus[ISMC_MAXL];
+    float mut[ISMC_MAXL];
+    float g[ISMC_MAXL];
+    float d[ISMC_MAXL];
+} ismc_stack;
+
+/*
+ * Sphere geometry with the reference's argument meaning (ISMC.py:164-165):
+ * R/T = sphere present; pw = wall reflectance; fs/fp/fd = sample, source
+ * (R) or optional (T) port and detector AREA fractions; f = total port
+ * fraction; *_angle = acceptance half-angle in RADIANS used when that sphere
+ * is absent (ISMC.py:221-236); specular_included tilts the beam to mu_z=0.99
+ * (ISMC.py:177-179).
+ */
+typedef struct ismc_spheres {
+    uint8_t R, T, specular_included, _pad0[5];
+    double R_pw, R_fs, R_fp, R_fd, R_f, R_angle;
+    double T_pw, T_fs, T_fp, T_fd, T_f, T_angle;
+} ismc_spheres;
+
+/* One simulation instance of a batch. */
+typedef struct ismc_instance {
+    ismc_stack stack;
+    ismc_spheres spheres;
+    uint64_t n_packets;       /* packets to launch */
+    uint64_t packet_offset;   /* id of the first packet (sharding / resume) */
+    uint64_t seed;            /* Philox key */
+    uint32_t stream;          /* Philox stream id (independent streams per seed) */
+    uint32_t mode;            /* ISMC_MODE_* */
+    float roulette_threshold; /* 1e-4 as in MLMC.py:86, 1e-3 as in ISMC.py:136 */
+    float roulette_m;         /* survival 1/m, weight *m (10 in the reference) */
+} ismc_instance;
+
+/*
+ * Result of one instance.  sum[k] = sum over packets of round(x_k * 2^scale_log2)
+ * and sumsq[k] = sum of round(x_k^2 * 2^scale_log2), where x_k is the packet's
+ * weight scored into tally k (ISMC_T_*).  Fractions of N as the reference
+ * returns them (ISMC.py:406) are sum[k] / (n * 2^scale_log2).
+ */
+typedef struct ismc_tally {
+    uint64_t n;               /* packets simulated */
+    uint64_t sum[5];
+    uint64_t sumsq[5];
+    uint64_t steps;           /* free-path draws in scattering layers */
+    uint64_t events;          /* propagation events (steps, boundary hits, incidences) */
+    uint64_t reincidences;    /* sphere re-incidences */
+    uint64_t capped;          /* packets stopped by the event cap */
+    uint32_t scale_log2;
+    int32_t status;           /* ISMC_OK or ISMC_ERR_STEP_LIMIT */
+    float analytic_specular;  /* deterministic specular reflectance of the stack (see ismc_run) */
+    float analytic_ballistic; /* deterministic unscattered transmittance (normal incidence) */
+} ismc_tally;
+
+/* Launch tuning; pass NULL to use the context's autotuned choice. */
+typedef struct ismc_tune {
+    uint32_t block_threads;   /* threads per block (multiple of 32, <= 512) */
+    uint32_t blocks_per_sm;   /* resident blocks per SM requested (0 = occupancy max) */
+    uint32_t chunk_packets;   /* packets a warp claims from the work queue at once */
+    uint32_t max_events;      /* per-packet event cap (0 = default 10,000,000) */
+} ismc_tune;
+
+typedef struct ismc_ctx ismc_ctx;
+
+/* ABI version (ISMC_ABI_VERSION). */
+int ismc_version(void);
+
+/* Create a context on a CUDA device.  Replaces the per-call cudaSetDevice +
+ * curand state set-up of CUDA/CUDAISMLMC.h:660-683. */
+int ismc_init(int device, ismc_ctx** out);
+
+/* Release a context and everything it owns. */
+int ismc_destroy(ismc_ctx* ctx);
+
+/*
+ * One forward simulation: replaces ISMC.py:164 ISMC() / ISMLMC.py:101 ISMLMC()
+ * and the CUDA host wrapper CUDA/CUDAISMLMC.h:656 ISMLMC().  The reference's
+ * roulette threshold of MLMC.py:86 (1e-4) and m = 10 are used; for the single
+ * slab driver's 1e-3 (ISMC.py:136) use ismc_run_batch with one instance.
+ * Host pointers in, host tally out; blocks until the result is ready.
+ */
+int ismc_run(ismc_ctx* ctx, const ismc_stack* stack, const ismc_spheres* sph,
+             uint64_t n_packets, uint64_t seed, uint32_t mode, ismc_tally* out);
+
+/*
+ * Many independent simulations of uneven size in one persistent launch,
+ * drained from a device work queue.  Replaces the per-grid-point loop of
+ * CUDA/ISMLMC-lookup.cu:153-421 (singleLayerSampleSpace), lookup.py:228-259
+ * (sample_space) and the per-objective launches of
+ * CUDA/ISMLMC-minimization.cu:89-131 (cost).  out has n_inst entries.
+ */
+int ismc_run_batch(ismc_ctx* ctx, const ismc_instance* inst, uint32_t n_inst,
+                   const ismc_tune* tune, ismc_tally* out);
+
+/*
+ * Device-pointer variant for callers whose instances are already resident on
+ * the GPU: d_inst and d_out are device pointers (n_inst entries), stream is a
+ * cudaStream_t (NULL = the context's stream).  Asynchronous: returns after
+ * enqueueing.  Used for graph capture and by callers that keep data in HBM.
+ */
+int ismc_run_batch_device(ismc_ctx* ctx, const ismc_instance* d_inst, uint32_t n_inst,
+                          const ismc_tune* tune, ismc_tally* d_out, void* stream);
+
+/* Choose block size / chunk size for a representative batch by timing short
+ * trial launches; the choice is stored in the context and returned in *out. */
+int ismc_autotune(ismc_ctx* ctx, const ismc_instance* inst, uint32_t n_inst,
+                  ismc_tune* out);
+
+/* Copy the last error message of ctx (or of the library when ctx is NULL). */
+int ismc_last_error(const ismc_ctx* ctx, char* buf, size_t n);
+
+/* Sizes of the ABI structs, so bindings can check their own layouts. */
+size_t ismc_sizeof(int which);   /* 0 stack, 1 spheres, 2 instance, 3 tally, 4 tune */
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ISMC_GB300_H */

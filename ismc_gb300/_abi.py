@@ -1,0 +1,102 @@
+"""ctypes mirror of the C ABI in include/ismc.h.
+
+The struct layouts here are checked against the library's own ``ismc_sizeof``
+when the library is loaded, so a mismatch fails loudly instead of corrupting
+memory.
+"""
+import ctypes as C
+
+MAXL = 16
+ABI_VERSION = 1
+
+OK = 0
+ERR_INVALID_ARG = -1
+ERR_CUDA = -2
+ERR_STEP_LIMIT = -3
+ERR_NO_DEVICE = -4
+ERR_ALLOC = -5
+ERR_CAPACITY = -6
+ERR_INTERNAL = -7
+ERR_NAMES = {0: "OK", -1: "INVALID_ARG", -2: "CUDA", -3: "STEP_LIMIT", -4: "NO_DEVICE",
+             -5: "ALLOC", -6: "CAPACITY", -7: "INTERNAL"}
+
+MODE_COMPAT = 0
+MODE_PHYSICAL = 1
+
+# tally order = the reference's return order (ISMC.py:406)
+TALLIES = ("A", "R_d", "R_s", "T_d", "T_u")
+
+
+class Stack(C.Structure):
+    _fields_ = [("L", C.c_uint32), ("_pad0", C.c_uint32),
+                ("n", C.c_float * MAXL), ("mua", C.c_float * MAXL), ("mus", C.c_float * MAXL),
+                ("mut", C.c_float * MAXL), ("g", C.c_float * MAXL), ("d", C.c_float * MAXL)]
+
+
+class Spheres(C.Structure):
+    _fields_ = [("R", C.c_uint8), ("T", C.c_uint8), ("specular_included", C.c_uint8),
+                ("_pad0", C.c_uint8 * 5),
+                ("R_pw", C.c_double), ("R_fs", C.c_double), ("R_fp", C.c_double),
+                ("R_fd", C.c_double), ("R_f", C.c_double), ("R_angle", C.c_double),
+                ("T_pw", C.c_double), ("T_fs", C.c_double), ("T_fp", C.c_double),
+                ("T_fd", C.c_double), ("T_f", C.c_double), ("T_angle", C.c_double)]
+
+
+class Instance(C.Structure):
+    _fields_ = [("stack", Stack), ("spheres", Spheres), ("n_packets", C.c_uint64),
+                ("packet_offset", C.c_uint64), ("seed", C.c_uint64), ("stream", C.c_uint32),
+                ("mode", C.c_uint32), ("roulette_threshold", C.c_float),
+                ("roulette_m", C.c_float)]
+
+
+class Tally(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("sum", C.c_uint64 * 5), ("sumsq", C.c_uint64 * 5),
+                ("steps", C.c_uint64), ("events", C.c_uint64), ("reincidences", C.c_uint64),
+                ("capped", C.c_uint64), ("scale_log2", C.c_uint32), ("status", C.c_int32),
+                ("analytic_specular", C.c_float), ("analytic_ballistic", C.c_float)]
+
+
+class Tune(C.Structure):
+    _fields_ = [("block_threads", C.c_uint32), ("blocks_per_sm", C.c_uint32),
+                ("chunk_packets", C.c_uint32), ("max_events", C.c_uint32)]
+
+
+SIZEOF_INDEX = {0: Stack, 1: Spheres, 2: Instance, 3: Tally, 4: Tune}
+
+# every symbol include/ismc.h declares
+EXPORTS = ("ismc_version", "ismc_init", "ismc_destroy", "ismc_run", "ismc_run_batch",
+           "ismc_run_batch_device", "ismc_autotune", "ismc_last_error", "ismc_sizeof")
+
+
+def declare(lib):
+    """Attach argtypes/restype to the library's entry points."""
+    P = C.POINTER
+    lib.ismc_version.restype = C.c_int
+    lib.ismc_version.argtypes = []
+    lib.ismc_init.restype = C.c_int
+    lib.ismc_init.argtypes = [C.c_int, P(C.c_void_p)]
+    lib.ismc_destroy.restype = C.c_int
+    lib.ismc_destroy.argtypes = [C.c_void_p]
+    lib.ismc_run.restype = C.c_int
+    lib.ismc_run.argtypes = [C.c_void_p, P(Stack), P(Spheres), C.c_uint64, C.c_uint64, C.c_uint32,
+                             P(Tally)]
+    lib.ismc_run_batch.restype = C.c_int
+    lib.ismc_run_batch.argtypes = [C.c_void_p, P(Instance), C.c_uint32, P(Tune), P(Tally)]
+    lib.ismc_run_batch_device.restype = C.c_int
+    lib.ismc_run_batch_device.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, P(Tune), C.c_void_p,
+                                          C.c_void_p]
+    lib.ismc_autotune.restype = C.c_int
+    lib.ismc_autotune.argtypes = [C.c_void_p, P(Instance), C.c_uint32, P(Tune)]
+    lib.ismc_last_error.restype = C.c_int
+    lib.ismc_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
+    lib.ismc_sizeof.restype = C.c_size_t
+    lib.ismc_sizeof.argtypes = [C.c_int]
+    for k, cls in SIZEOF_INDEX.items():
+        got = lib.ismc_sizeof(k)
+        if got != C.sizeof(cls):
+            raise RuntimeError(f"ABI mismatch for {cls.__name__}: library {got} B, ctypes "
+                               f"{C.sizeof(cls)} B")
+    v = lib.ismc_version()
+    if v != ABI_VERSION:
+        raise RuntimeError(f"libismc ABI version {v}, bindings expect {ABI_VERSION}")
+    return lib

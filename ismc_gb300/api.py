@@ -1,0 +1,320 @@
+"""Python host API over the C ABI (include/ismc.h).
+
+This is the layer the reference's callers reach through the drop-in modules
+(``ismc_gb300.dropin.ISMC`` / ``ISMLMC``) and the batch drivers.  It builds the
+ABI structs, calls ``libismc.so`` and turns integer tallies into FP64 means and
+standard errors.  There is no CPU fallback: without the CUDA library or a GPU
+every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import threading
+from dataclasses import dataclass, field
+from typing import Iterable, List, Optional, Sequence
+
+from . import _abi
+
+_LIB = None
+_LIB_LOCK = threading.Lock()
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libismc.so")
+
+
+class IsmcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"ismc error {code} ({_abi.ERR_NAMES.get(code, '?')}): {msg}")
+        self.code = code
+
+
+def load_library(path: str = LIB_PATH):
+    """Load and check libismc.so (built in-tree by ``python -m ismc_gb300.build``)."""
+    global _LIB
+    with _LIB_LOCK:
+        if _LIB is None:
+            if not os.path.exists(path):
+                raise RuntimeError(f"{path} is missing: build it with `python -m ismc_gb300.build`"
+                                   " (the GPU path has no CPU fallback)")
+            _LIB = _abi.declare(C.CDLL(path))
+        return _LIB
+
+
+# ----------------------------------------------------------------------------
+# inputs
+# ----------------------------------------------------------------------------
+@dataclass
+class Layer:
+    """One layer: refractive index, absorption and scattering coefficients (1/cm),
+    anisotropy g and thickness d (cm).  mus == 0 marks a non-scattering slide.
+    mut defaults to mua + mus, as the reference's callers pass it
+    (lookup.py:238, minimization.py:205)."""
+    n: float
+    mua: float
+    mus: float
+    g: float
+    d: float
+    mut: Optional[float] = None
+
+    @staticmethod
+    def slide(n=1.5, d=0.1):
+        return Layer(n, 0.0, 0.0, 0.0, d)
+
+    @staticmethod
+    def from_reduced(n, mua, mus_reduced, g, d):
+        """mu_s from the reduced coefficient: mu_s = mu_s' / (1 - g), or mu_s' when g == 1
+        (ISMC.py:28-29)."""
+        mus = mus_reduced if g == 1 else mus_reduced / (1.0 - g)
+        return Layer(n, mua, mus, g, d)
+
+
+def cap_fraction(port_radius, sphere_radius):
+    """Area fraction of a circular port on a sphere (spherical cap):
+    f = (1 - sqrt(1 - (a/Rs)^2)) / 2."""
+    return 0.5 * (1.0 - math.sqrt(1.0 - (port_radius / sphere_radius) ** 2))
+
+
+@dataclass
+class Spheres:
+    """Two-sphere geometry with the reference's argument meaning (ISMC.py:34-50).
+    Angles in radians."""
+    R: bool = True
+    R_pw: float = 0.99
+    R_fs: float = 0.02351
+    R_fp: float = 0.054638
+    R_fd: float = 0.02351
+    R_f: Optional[float] = None
+    R_angle: float = math.pi / 10
+    specular_included: bool = False
+    T: bool = False
+    T_pw: float = 0.99
+    T_fs: float = 0.054638
+    T_fp: float = 0.02351
+    T_fd: float = 0.02351
+    T_f: Optional[float] = None
+    T_angle: float = 0.22 * math.pi / 180
+
+    def __post_init__(self):
+        if self.R_f is None:
+            self.R_f = self.R_fs + self.R_fp + self.R_fd
+        if self.T_f is None:
+            self.T_f = self.T_fs + self.T_fp + self.T_fd
+
+    @staticmethod
+    def from_radii(sphere_radius=5.08, sample_port=1.27, entrance_port=1.27, detector_port=0.635,
+                   wall=0.98, R=True, T=True, specular_included=False,
+                   R_angle=math.pi / 10, T_angle=0.22 * math.pi / 180):
+        """Port radii (cm) -> the reference's area fractions; the T sphere's
+        optional port takes the entrance-port size."""
+        fs = cap_fraction(sample_port, sphere_radius)
+        fp = cap_fraction(entrance_port, sphere_radius)
+        fd = cap_fraction(detector_port, sphere_radius)
+        return Spheres(R=R, R_pw=wall, R_fs=fs, R_fp=fp, R_fd=fd, R_angle=R_angle,
+                       specular_included=specular_included, T=T, T_pw=wall, T_fs=fs, T_fp=fp,
+                       T_fd=fd, T_angle=T_angle)
+
+
+def make_stack(layers: Sequence[Layer]) -> _abi.Stack:
+    if not 1 <= len(layers) <= _abi.MAXL:
+        raise ValueError(f"a stack has 1..{_abi.MAXL} layers, got {len(layers)}")
+    s = _abi.Stack()
+    s.L = len(layers)
+    for i, ly in enumerate(layers):
+        s.n[i] = ly.n
+        s.mua[i] = ly.mua
+        s.mus[i] = ly.mus
+        s.mut[i] = ly.mua + ly.mus if ly.mut is None else ly.mut
+        s.g[i] = ly.g
+        s.d[i] = ly.d
+    return s
+
+
+def make_spheres(sp: Spheres) -> _abi.Spheres:
+    x = _abi.Spheres()
+    x.R = 1 if sp.R else 0
+    x.T = 1 if sp.T else 0
+    x.specular_included = 1 if sp.specular_included else 0
+    for k in ("R_pw", "R_fs", "R_fp", "R_fd", "R_f", "R_angle",
+              "T_pw", "T_fs", "T_fp", "T_fd", "T_f", "T_angle"):
+        setattr(x, k, float(getattr(sp, k)))
+    return x
+
+
+MODES = {"compat": _abi.MODE_COMPAT, "physical": _abi.MODE_PHYSICAL,
+         _abi.MODE_COMPAT: _abi.MODE_COMPAT, _abi.MODE_PHYSICAL: _abi.MODE_PHYSICAL}
+
+
+def make_instance(layers: Sequence[Layer], spheres: Spheres, n_packets: int, seed: int = 0,
+                  stream: int = 0, mode="compat", roulette_threshold: float = 1e-4,
+                  roulette_m: float = 10.0, packet_offset: int = 0) -> _abi.Instance:
+    """One simulation instance.  roulette_threshold 1e-4 / m = 10 are MLMC.py:86-87;
+    the single-slab driver of ISMC.py:136 uses 1e-3."""
+    inst = _abi.Instance()
+    inst.stack = make_stack(layers)
+    inst.spheres = make_spheres(spheres)
+    inst.n_packets = int(n_packets)
+    inst.packet_offset = int(packet_offset)
+    inst.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    inst.stream = int(stream) & 0xFFFFFFFF
+    inst.mode = MODES[mode]
+    inst.roulette_threshold = roulette_threshold
+    inst.roulette_m = roulette_m
+    return inst
+
+
+def instance_array(instances: Sequence[_abi.Instance]):
+    arr = (_abi.Instance * len(instances))()
+    for i, x in enumerate(instances):
+        arr[i] = x
+    return arr
+
+
+# ----------------------------------------------------------------------------
+# outputs
+# ----------------------------------------------------------------------------
+@dataclass
+class Result:
+    """Normalised outcome of one instance: fractions of N as the reference
+    returns them (ISMC.py:406), their standard errors, and counters."""
+    n: int
+    mean: List[float]
+    se: List[float]
+    status: int
+    steps: int
+    events: int
+    reincidences: int
+    capped: int
+    analytic_specular: float
+    analytic_ballistic: float
+    sums: List[int] = field(repr=False, default_factory=list)
+    sumsqs: List[int] = field(repr=False, default_factory=list)
+
+    def as_tuple(self):
+        return tuple(self.mean)
+
+    def __getitem__(self, name):
+        return self.mean[_abi.TALLIES.index(name)]
+
+
+def tally_to_result(t: _abi.Tally) -> Result:
+    """FP64 normalisation of the fixed-point sums: mean = S/(N 2^k),
+    SE = sqrt((Q/(N 2^k) - mean^2) / (N - 1))."""
+    n = int(t.n)
+    scale = float(2 ** int(t.scale_log2 or 32))
+    mean, se = [], []
+    for k in range(5):
+        s, q = int(t.sum[k]), int(t.sumsq[k])
+        if n > 0:
+            m = s / scale / n
+            ex2 = q / scale / n
+            var = max(ex2 - m * m, 0.0) * n / (n - 1) if n > 1 else 0.0
+            mean.append(m)
+            se.append(math.sqrt(var / n))
+        else:
+            mean.append(float("nan"))
+            se.append(float("nan"))
+    return Result(n=n, mean=mean, se=se, status=int(t.status), steps=int(t.steps),
+                  events=int(t.events), reincidences=int(t.reincidences), capped=int(t.capped),
+                  analytic_specular=float(t.analytic_specular),
+                  analytic_ballistic=float(t.analytic_ballistic),
+                  sums=[int(x) for x in t.sum], sumsqs=[int(x) for x in t.sumsq])
+
+
+def make_tune(block_threads=0, blocks_per_sm=0, chunk_packets=0, max_events=0):
+    return _abi.Tune(block_threads, blocks_per_sm, chunk_packets, max_events)
+
+
+# ----------------------------------------------------------------------------
+# engine
+# ----------------------------------------------------------------------------
+class Engine:
+    """A propagator context on one GPU (wraps ismc_init / ismc_destroy).
+
+    Not thread-safe: use one Engine per thread (or lock around it), as for the
+    C context."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        rc = self.lib.ismc_init(int(device), C.byref(h))
+        if rc != 0:
+            raise IsmcError(rc, self._err(None))
+        self.h = h
+        self.device = device
+
+    def _err(self, h):
+        buf = C.create_string_buffer(1024)
+        self.lib.ismc_last_error(h, buf, 1024)
+        return buf.value.decode(errors="replace")
+
+    def _check(self, rc):
+        if rc != 0:
+            raise IsmcError(rc, self._err(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ismc_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- single instance: ismc_run (MLMC.py roulette 1e-4 / m 10)
+    def run(self, layers: Sequence[Layer], spheres: Spheres, n_packets: int, seed: int = 0,
+            mode="compat") -> Result:
+        st = make_stack(layers)
+        sp = make_spheres(spheres)
+        out = _abi.Tally()
+        rc = self.lib.ismc_run(self.h, C.byref(st), C.byref(sp), int(n_packets), int(seed),
+                               MODES[mode], C.byref(out))
+        if rc not in (0, _abi.ERR_STEP_LIMIT):
+            self._check(rc)
+        return tally_to_result(out)
+
+    # -- many instances in one persistent launch: ismc_run_batch
+    def run_batch_raw(self, instances, tune: Optional[_abi.Tune] = None):
+        arr = instances if isinstance(instances, C.Array) else instance_array(instances)
+        n = len(arr)
+        out = (_abi.Tally * n)()
+        rc = self.lib.ismc_run_batch(self.h, arr, n, C.byref(tune) if tune else None, out)
+        self._check(rc)
+        return out
+
+    def run_batch(self, instances, tune: Optional[_abi.Tune] = None) -> List[Result]:
+        return [tally_to_result(t) for t in self.run_batch_raw(instances, tune)]
+
+    def run_batch_device(self, d_inst_ptr: int, n_inst: int, d_out_ptr: int, stream_ptr: int = 0,
+                         tune: Optional[_abi.Tune] = None):
+        """Enqueue a batch whose instances already live on the GPU (device pointers,
+        e.g. torch uint8 tensors' data_ptr()); asynchronous on `stream_ptr`."""
+        rc = self.lib.ismc_run_batch_device(self.h, C.c_void_p(d_inst_ptr), int(n_inst),
+                                            C.byref(tune) if tune else None,
+                                            C.c_void_p(d_out_ptr), C.c_void_p(stream_ptr))
+        self._check(rc)
+
+    def autotune(self, instances) -> _abi.Tune:
+        arr = instances if isinstance(instances, C.Array) else instance_array(instances)
+        t = _abi.Tune()
+        self._check(self.lib.ismc_autotune(self.h, arr, len(arr), C.byref(t)))
+        return t
+
+
+_DEFAULT = {}
+
+
+def default_engine(device: Optional[int] = None) -> Engine:
+    """Process-wide engine per device (device from ISMC_DEVICE, default 0)."""
+    dev = int(os.environ.get("ISMC_DEVICE", "0")) if device is None else int(device)
+    key = (dev, threading.get_ident())
+    if key not in _DEFAULT:
+        _DEFAULT[key] = Engine(dev)
+    return _DEFAULT[key]

@@ -1,0 +1,82 @@
+// ismc_dev.h -- device-side data layout of the propagator (shared by the
+// kernels and the host library; not part of the public ABI).
+#pragma once
+#include <stdint.h>
+#include "../../include/ismc.h"
+
+#define ISMC_HDR_WORDS 20
+#define ISMC_LAYER_FIELDS 14
+
+// Layer flags
+#define ISMC_LF_GLASS 1u   // mus == 0: no scattering (ISMLMC.py:81, MLMC.py:97)
+#define ISMC_LF_ISO   2u   // g == 0: isotropic phase function (MLMC.py:183)
+
+// Instance flags
+#define ISMC_IF_RSPHERE 1u
+#define ISMC_IF_TSPHERE 2u
+
+// Prepared instance: everything the walk needs, derived once per launch by
+// ismc_prepare_kernel.  Stored structure-of-arrays so that lanes reading the
+// same field of different layers hit distinct shared-memory banks.  One warp
+// copies it word by word into its shared-memory slot.
+struct DevInst {
+    // header: 20 words
+    uint32_t L, mode, flags, stream;
+    uint32_t seed_lo, seed_hi;
+    float t_tot;                // total thickness (bottom of the stack)
+    float cos_port[2];          // |mu_z| >= cos_port -> specular (R) / unscattered (T)
+    float p_reinc[2];           // sphere re-incidence probability (sphere multiplier)
+    float ux0, uz0;             // launch direction
+    float roul_thr, roul_m, roul_inv_m;
+    float eta_in[2];            // 1/n of the top / bottom layer (ambient -> sample)
+    uint32_t _hpad[2];
+    // per layer, MAXL each
+    float n[ISMC_MAXL];
+    float mut[ISMC_MAXL];
+    float inv_mut[ISMC_MAXL];
+    float drop[ISMC_MAXL];      // tissue: mua/mut per interaction; glass: mua (1/cm)
+    float hga[ISMC_MAXL];       // Henyey-Greenstein constants: 1/(2g)
+    float hgb[ISMC_MAXL];       //   1 + g^2
+    float hgc[ISMC_MAXL];       //   1 - g^2
+    float hgd[ISMC_MAXL];       //   1 - g
+    float hge[ISMC_MAXL];       //   2 g
+    float z_top[ISMC_MAXL];
+    float z_bot[ISMC_MAXL];
+    float eta_up[ISMC_MAXL];    // n[l] / n(above)   (ambient 1 above layer 0)
+    float eta_dn[ISMC_MAXL];    // n[l] / n(below)   (ambient 1 below layer L-1)
+    uint32_t lflags[ISMC_MAXL];
+};
+
+static_assert(sizeof(DevInst) == 4 * (ISMC_HDR_WORDS + ISMC_LAYER_FIELDS * ISMC_MAXL),
+              "DevInst layout");
+
+// Packet range of an instance (the queue decodes chunks from these).
+struct DevRange {
+    uint64_t offset;            // first packet id
+    uint64_t count;             // packets
+};
+
+// Tally block in device memory: same layout as ismc_tally so it can be copied
+// back verbatim.  Counters are added with 64-bit integer atomics.
+static_assert(sizeof(ismc_tally) == 8 * 15 + 4 * 4, "ismc_tally layout");
+
+struct PropParams {
+    const DevInst* inst;
+    const DevRange* range;
+    const unsigned long long* chunk_prefix;   // n_inst + 1 entries
+    ismc_tally* tally;
+    unsigned long long* queue_head;
+    uint32_t n_inst;
+    uint32_t chunk_packets;
+    uint32_t max_events;
+    uint32_t _pad;
+};
+
+// Host-callable launchers (defined in ismc_kernels.cu).
+extern "C++" {
+int ismc_launch_prepare(const ismc_instance* d_in, uint32_t n_inst, DevInst* d_inst,
+                        DevRange* d_range, unsigned long long* d_prefix, ismc_tally* d_out,
+                        uint32_t chunk_packets, unsigned long long* d_queue, void* stream);
+int ismc_launch_propagate(const PropParams& p, uint32_t blocks, uint32_t threads, void* stream);
+int ismc_propagate_occupancy(uint32_t threads, int* blocks_per_sm);
+}
