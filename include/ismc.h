@@ -121,6 +121,10 @@ typedef struct ismc_tally {
     uint64_t events;          /* propagation events (steps, boundary hits, incidences) */
     uint64_t reincidences;    /* sphere re-incidences */
     uint64_t capped;          /* packets stopped by the event cap */
+    uint64_t trapped;         /* packets refracted into a slide at a direction that
+                                 both faces totally reflect (a rounding artefact of
+                                 near-grazing entry, ~1e-7 per entry): their weight
+                                 is dropped instead of bouncing forever */
     uint32_t scale_log2;
     int32_t status;           /* ISMC_OK or ISMC_ERR_STEP_LIMIT */
     float analytic_specular;  /* deterministic specular reflectance of the stack (see ismc_run) */
@@ -169,9 +173,12 @@ int ismc_run_batch(ismc_ctx* ctx, const ismc_instance* inst, uint32_t n_inst,
 
 /*
  * Device-pointer variant for callers whose instances are already resident on
- * the GPU: d_inst and d_out are device pointers (n_inst entries), stream is a
- * cudaStream_t (NULL = the context's stream).  Asynchronous: returns after
- * enqueueing.  Used for graph capture and by callers that keep data in HBM.
+ * the GPU: d_inst and d_out are device pointers (n_inst entries), stream is the
+ * cudaStream_t to launch on, used as given (NULL = the legacy default stream).
+ * Asynchronous: returns after enqueueing.  The context's device buffers are
+ * reused by the next call, so calls on one context must not overlap on the GPU
+ * (enqueue them on one stream).  Used for graph capture and by callers that
+ * keep data in HBM.
  */
 int ismc_run_batch_device(ismc_ctx* ctx, const ismc_instance* d_inst, uint32_t n_inst,
                           const ismc_tune* tune, ismc_tally* d_out, void* stream);
@@ -184,8 +191,53 @@ int ismc_autotune(ismc_ctx* ctx, const ismc_instance* inst, uint32_t n_inst,
 /* Copy the last error message of ctx (or of the library when ctx is NULL). */
 int ismc_last_error(const ismc_ctx* ctx, char* buf, size_t n);
 
+/* ------------------------------------------------------------------------
+ * Inverse solver (plain path): PRAXIS minimisation of the reference's cost
+ *   sqrt( ((R_d-M_R)/M_R)^2 + (R_s-M_S)^2 + ((T_d-M_T)/M_T)^2 + (T_u-M_U)^2 )
+ * over (mu_a, mu_s') of one layer, each objective a GPU Monte Carlo run
+ * (minimization.py:201-238, CUDA/ISMLMC-minimization.cu:89-131 and :476).
+ * Many solves advance in lockstep: every round of objective evaluations of all
+ * active solves is ONE batched launch.
+ * ------------------------------------------------------------------------ */
+typedef struct ismc_solve_req {
+    ismc_instance base;       /* stack, spheres, packets per objective, seed, mode, roulette */
+    uint32_t layer;           /* layer whose (mu_a, mu_s') are unknown; its g is kept */
+    uint32_t separate;        /* 1: R-only, T-only and sphere-less runs per objective
+                                 (minimization.py:209-225); 0: one run with both spheres */
+    uint32_t log_coords;      /* 1: minimise over (ln mu_a, ln mu_s'); 0: over (mu_a, mu_s') */
+    uint32_t max_evals;       /* objective evaluations per minimisation (0 = 2000) */
+    uint32_t max_restarts;    /* re-runs when the result leaves the box (minimization.py:260-271) */
+    uint32_t fresh_streams;   /* 0: every evaluation of a solve reuses its Philox stream (common
+                                 random numbers, a deterministic objective); 1: a new stream per
+                                 evaluation, like the reference's global random state */
+    double meas[4];           /* measured R_d, R_s, T_d, T_u; NaN = not measured */
+    double x0[2];             /* initial (mu_a, mu_s') */
+    double lo[2], hi[2];      /* accepted box for (mu_a, mu_s') */
+    double h0, t0;            /* PRAXIS initial step and tolerance (in the chosen coordinates) */
+} ismc_solve_req;
+
+typedef struct ismc_solve_out {
+    double x[2];              /* recovered (mu_a, mu_s') */
+    double cost;              /* objective at x (last evaluation there) */
+    uint32_t evals;           /* objective evaluations, all restarts included */
+    uint32_t restarts;
+    int32_t status;           /* ISMC_OK, or ISMC_ERR_CAPACITY when every restart left the box */
+    uint32_t rounds;          /* batched launches this solve took part in */
+} ismc_solve_out;
+
+/* Solve n independent inverse problems; out has n entries. */
+int ismc_solve_batch(ismc_ctx* ctx, const ismc_solve_req* req, uint32_t n,
+                     ismc_solve_out* out);
+
+/* PRAXIS on a host callback, no GPU involved (n <= 8 variables).  Returns the
+ * minimum in *fmin and the number of evaluations in *nevals. */
+typedef double (*ismc_objective)(const double* x, int n, void* user);
+int ismc_praxis(ismc_objective f, void* user, int n, double* x, double t0, double h0,
+                int maxfun, double* fmin, int* nevals);
+
 /* Sizes of the ABI structs, so bindings can check their own layouts. */
-size_t ismc_sizeof(int which);   /* 0 stack, 1 spheres, 2 instance, 3 tally, 4 tune */
+size_t ismc_sizeof(int which);   /* 0 stack, 1 spheres, 2 instance, 3 tally, 4 tune,
+                                    5 solve_req, 6 solve_out */
 
 #ifdef __cplusplus
 }

@@ -52,7 +52,7 @@ class Instance(C.Structure):
 class Tally(C.Structure):
     _fields_ = [("n", C.c_uint64), ("sum", C.c_uint64 * 5), ("sumsq", C.c_uint64 * 5),
                 ("steps", C.c_uint64), ("events", C.c_uint64), ("reincidences", C.c_uint64),
-                ("capped", C.c_uint64), ("scale_log2", C.c_uint32), ("status", C.c_int32),
+                ("capped", C.c_uint64), ("trapped", C.c_uint64), ("scale_log2", C.c_uint32), ("status", C.c_int32),
                 ("analytic_specular", C.c_float), ("analytic_ballistic", C.c_float)]
 
 
@@ -61,11 +61,27 @@ class Tune(C.Structure):
                 ("chunk_packets", C.c_uint32), ("max_events", C.c_uint32)]
 
 
-SIZEOF_INDEX = {0: Stack, 1: Spheres, 2: Instance, 3: Tally, 4: Tune}
+class SolveReq(C.Structure):
+    _fields_ = [("base", Instance), ("layer", C.c_uint32), ("separate", C.c_uint32),
+                ("log_coords", C.c_uint32), ("max_evals", C.c_uint32),
+                ("max_restarts", C.c_uint32), ("fresh_streams", C.c_uint32),
+                ("meas", C.c_double * 4), ("x0", C.c_double * 2), ("lo", C.c_double * 2),
+                ("hi", C.c_double * 2), ("h0", C.c_double), ("t0", C.c_double)]
+
+
+class SolveOut(C.Structure):
+    _fields_ = [("x", C.c_double * 2), ("cost", C.c_double), ("evals", C.c_uint32),
+                ("restarts", C.c_uint32), ("status", C.c_int32), ("rounds", C.c_uint32)]
+
+
+OBJECTIVE = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_int, C.c_void_p)
+
+SIZEOF_INDEX = {0: Stack, 1: Spheres, 2: Instance, 3: Tally, 4: Tune, 5: SolveReq, 6: SolveOut}
 
 # every symbol include/ismc.h declares
 EXPORTS = ("ismc_version", "ismc_init", "ismc_destroy", "ismc_run", "ismc_run_batch",
-           "ismc_run_batch_device", "ismc_autotune", "ismc_last_error", "ismc_sizeof")
+           "ismc_run_batch_device", "ismc_autotune", "ismc_last_error", "ismc_sizeof",
+           "ismc_solve_batch", "ismc_praxis")
 
 
 def declare(lib):
@@ -89,6 +105,11 @@ def declare(lib):
     lib.ismc_autotune.argtypes = [C.c_void_p, P(Instance), C.c_uint32, P(Tune)]
     lib.ismc_last_error.restype = C.c_int
     lib.ismc_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
+    lib.ismc_solve_batch.restype = C.c_int
+    lib.ismc_solve_batch.argtypes = [C.c_void_p, P(SolveReq), C.c_uint32, P(SolveOut)]
+    lib.ismc_praxis.restype = C.c_int
+    lib.ismc_praxis.argtypes = [OBJECTIVE, C.c_void_p, C.c_int, P(C.c_double), C.c_double,
+                                C.c_double, C.c_int, P(C.c_double), P(C.c_int)]
     lib.ismc_sizeof.restype = C.c_size_t
     lib.ismc_sizeof.argtypes = [C.c_int]
     for k, cls in SIZEOF_INDEX.items():

@@ -184,6 +184,7 @@ class Result:
     events: int
     reincidences: int
     capped: int
+    trapped: int
     analytic_specular: float
     analytic_ballistic: float
     sums: List[int] = field(repr=False, default_factory=list)
@@ -215,9 +216,42 @@ def tally_to_result(t: _abi.Tally) -> Result:
             se.append(float("nan"))
     return Result(n=n, mean=mean, se=se, status=int(t.status), steps=int(t.steps),
                   events=int(t.events), reincidences=int(t.reincidences), capped=int(t.capped),
+                  trapped=int(t.trapped),
                   analytic_specular=float(t.analytic_specular),
                   analytic_ballistic=float(t.analytic_ballistic),
                   sums=[int(x) for x in t.sum], sumsqs=[int(x) for x in t.sumsq])
+
+
+def make_solve(layers: Sequence[Layer], layer: int, spheres: Spheres, n_packets: int,
+               meas, x0, lo=(1e-6, 1e-6), hi=(1e6, 1e6), seed: int = 0, separate=False,
+               log_coords=True, h0=None, t0=None, max_evals=400, max_restarts=3,
+               mode="compat", roulette_threshold=1e-4, fresh_streams=False) -> _abi.SolveReq:
+    """One plain-path inverse problem: find (mu_a, mu_s') of `layer` so that the
+    simulated (R_d, R_s, T_d, T_u) match `meas` (None = not measured) under the
+    reference's cost (minimization.py:231-238).  In log coordinates the PRAXIS
+    step/tolerance default to 0.5 / 1e-3 (relative), else to the reference's
+    example values 5 / 0.1 (Minimization/example.ini [minimization]).
+    fresh_streams=False gives every evaluation of one solve the same Philox
+    stream (common random numbers: the objective is then a deterministic
+    function of the parameters); True draws a new stream per evaluation, as the
+    reference's global random state does."""
+    r = _abi.SolveReq()
+    r.base = make_instance(layers, spheres, n_packets, seed=seed, mode=mode,
+                           roulette_threshold=roulette_threshold)
+    r.layer = int(layer)
+    r.separate = 1 if separate else 0
+    r.log_coords = 1 if log_coords else 0
+    r.max_evals = int(max_evals)
+    r.max_restarts = int(max_restarts)
+    r.fresh_streams = 1 if fresh_streams else 0
+    for k in range(4):
+        r.meas[k] = float("nan") if meas[k] is None else float(meas[k])
+    r.x0[0], r.x0[1] = float(x0[0]), float(x0[1])
+    r.lo[0], r.lo[1] = float(lo[0]), float(lo[1])
+    r.hi[0], r.hi[1] = float(hi[0]), float(hi[1])
+    r.h0 = float(h0 if h0 is not None else (0.5 if log_coords else 5.0))
+    r.t0 = float(t0 if t0 is not None else (1e-3 if log_coords else 0.1))
+    return r
 
 
 def make_tune(block_threads=0, blocks_per_sm=0, chunk_packets=0, max_events=0):
@@ -300,6 +334,14 @@ class Engine:
                                             C.byref(tune) if tune else None,
                                             C.c_void_p(d_out_ptr), C.c_void_p(stream_ptr))
         self._check(rc)
+
+    def solve_batch(self, requests) -> List[_abi.SolveOut]:
+        """Batched plain-path inverse solves (ismc_solve_batch): every round of
+        objective evaluations of all active solves is one GPU launch."""
+        arr = requests if isinstance(requests, C.Array) else (_abi.SolveReq * len(requests))(*requests)
+        out = (_abi.SolveOut * len(arr))()
+        self._check(self.lib.ismc_solve_batch(self.h, arr, len(arr), out))
+        return list(out)
 
     def autotune(self, instances) -> _abi.Tune:
         arr = instances if isinstance(instances, C.Array) else instance_array(instances)

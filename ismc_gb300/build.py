@@ -24,7 +24,9 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + os.path.join(ROOT, "include")] + ARCH
 
-SOURCES = ["ismc_kernels.cu", "ismc_capi.cu"]
+SOURCES = ["ismc_kernels.cu", "ismc_capi.cu", "ismc_praxis.cpp", "ismc_solve.cpp"]
+CXX_FLAGS = ["-O2", "-std=c++20", "-fPIC", "-ffp-contract=off", "-Wall",
+             "-I" + os.path.join(ROOT, "include")]
 
 
 def nvcc():
@@ -49,9 +51,12 @@ def _compile(src, verbose_ptxas=False):
     srcp = os.path.join(CSRC, src)
     if _newer(obj, [srcp, __file__] + _headers()) and not verbose_ptxas:
         return obj, ""
-    cmd = [nvcc(), "-c", srcp, "-o", obj] + NVCC_FLAGS
-    if verbose_ptxas:
-        cmd += ["-Xptxas", "-v"]
+    if src.endswith(".cpp"):
+        cmd = [os.environ.get("CXX", "g++"), "-c", srcp, "-o", obj] + CXX_FLAGS
+    else:
+        cmd = [nvcc(), "-c", srcp, "-o", obj] + NVCC_FLAGS
+        if verbose_ptxas:
+            cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
@@ -65,7 +70,7 @@ def build(verbose_ptxas=False, quiet=True):
     objs = [o for o, _ in res]
     logs = "".join(l for _, l in res)
     if not _newer(LIB, objs):
-        cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-lcudart"]
+        cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-lcudart", "-lstdc++"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

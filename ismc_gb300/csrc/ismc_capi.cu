@@ -27,18 +27,19 @@ struct ismc_ctx {
     DevRange* d_range = nullptr;
     unsigned long long* d_prefix = nullptr;
     ismc_tally* d_out = nullptr;
-    unsigned long long* d_queue = nullptr;
+    unsigned long long* d_ctrl = nullptr;     // [0] queue head, [1] packets per chunk
     // pinned staging
     ismc_instance* h_in = nullptr;
     ismc_tally* h_out = nullptr;
     // launch shape
     ismc_tune tune{256, 0, 0, 0};
+    uint32_t chunks_per_warp = 8;   // queue chunks per warp when sized on the device
     bool tuned = false;
     // graph of the host-pointer pipeline
     cudaGraphExec_t gexec = nullptr;
     uint32_t g_n = 0;
     ismc_tune g_tune{0, 0, 0, 0};
-    uint64_t g_total = 0;
+    uint32_t g_cpw = 0;
     char err[512] = {0};
 };
 
@@ -72,6 +73,8 @@ extern "C" size_t ismc_sizeof(int which) {
         case 2: return sizeof(ismc_instance);
         case 3: return sizeof(ismc_tally);
         case 4: return sizeof(ismc_tune);
+        case 5: return sizeof(ismc_solve_req);
+        case 6: return sizeof(ismc_solve_out);
         default: return 0;
     }
 }
@@ -124,7 +127,7 @@ extern "C" int ismc_init(int device, ismc_ctx** out) {
         if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
             rc = ISMC_ERR_CUDA; break;
         }
-        if (cudaMalloc(&ctx->d_queue, sizeof(unsigned long long)) != cudaSuccess) {
+        if (cudaMalloc(&ctx->d_ctrl, 2 * sizeof(unsigned long long)) != cudaSuccess) {
             rc = ISMC_ERR_CUDA; break;
         }
         int bps = 0;
@@ -134,7 +137,7 @@ extern "C" int ismc_init(int device, ismc_ctx** out) {
         set_err(nullptr, rc, "ismc_init: CUDA set-up failed on device %d: %s", device,
                 cudaGetErrorString(cudaGetLastError()));
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
-        cudaFree(ctx->d_queue);
+        cudaFree(ctx->d_ctrl);
         delete ctx;
         return rc;
     }
@@ -147,7 +150,7 @@ extern "C" int ismc_destroy(ismc_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     release_buffers(ctx);
-    cudaFree(ctx->d_queue);
+    cudaFree(ctx->d_ctrl);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return 0;
@@ -169,9 +172,10 @@ static uint64_t total_packets(const ismc_instance* in, uint32_t n) {
     return t;
 }
 
-// Resolve a (possibly partial) tune request into a concrete launch.
-static int resolve_tune(ismc_ctx* ctx, const ismc_tune* req, uint64_t total, ismc_tune* t,
-                        uint32_t* blocks) {
+// Resolve a (possibly partial) tune request into a concrete launch.  A zero
+// chunk_packets is left zero: the scan kernel then sizes chunks on the device
+// from the batch's total packet count (ctx->chunks_per_warp chunks per warp).
+static int resolve_tune(ismc_ctx* ctx, const ismc_tune* req, ismc_tune* t, uint32_t* blocks) {
     ismc_tune x = req ? *req : ctx->tune;
     if (x.block_threads == 0) x.block_threads = ctx->tune.block_threads ? ctx->tune.block_threads : 256;
     if (x.block_threads % 32 || x.block_threads > 512)
@@ -182,13 +186,6 @@ static int resolve_tune(ismc_ctx* ctx, const ismc_tune* req, uint64_t total, ism
         return set_err(ctx, ISMC_ERR_CUDA, "occupancy query failed for %u threads", x.block_threads);
     uint32_t want = x.blocks_per_sm ? std::min<uint32_t>(x.blocks_per_sm, (uint32_t)bps) : (uint32_t)bps;
     x.blocks_per_sm = want;
-    if (x.chunk_packets == 0) {
-        // enough chunks for every warp to claim several
-        const uint64_t warps = (uint64_t)ctx->sms * want * (x.block_threads / 32);
-        uint64_t c = total / (warps * 8 + 1);
-        c = std::max<uint64_t>(32, std::min<uint64_t>(c, 8192));
-        x.chunk_packets = (uint32_t)((c + 31) / 32 * 32);
-    }
     if (x.max_events == 0) x.max_events = kDefaultMaxEvents;
     *t = x;
     *blocks = (uint32_t)ctx->sms * want;
@@ -198,19 +195,19 @@ static int resolve_tune(ismc_ctx* ctx, const ismc_tune* req, uint64_t total, ism
 static int enqueue_pipeline(ismc_ctx* ctx, const ismc_instance* d_in, uint32_t n,
                             const ismc_tune& t, uint32_t blocks, ismc_tally* d_out,
                             cudaStream_t s) {
+    const uint32_t warps = blocks * (t.block_threads / 32);
     int rc = ismc_launch_prepare(d_in, n, ctx->d_inst, ctx->d_range, ctx->d_prefix, d_out,
-                                 t.chunk_packets, ctx->d_queue, (void*)s);
+                                 ctx->d_ctrl, t.chunk_packets, warps, ctx->chunks_per_warp,
+                                 (void*)s);
     if (rc) return set_err(ctx, rc, "prepare launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     PropParams p;
     p.inst = ctx->d_inst;
     p.range = ctx->d_range;
     p.chunk_prefix = ctx->d_prefix;
     p.tally = d_out;
-    p.queue_head = ctx->d_queue;
+    p.ctrl = ctx->d_ctrl;
     p.n_inst = n;
-    p.chunk_packets = t.chunk_packets;
     p.max_events = t.max_events;
-    p._pad = 0;
     rc = ismc_launch_propagate(p, blocks, t.block_threads, (void*)s);
     if (rc) return set_err(ctx, rc, "propagate launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     return 0;
@@ -248,12 +245,11 @@ extern "C" int ismc_run_batch_device(ismc_ctx* ctx, const ismc_instance* d_inst,
     if (rc) return rc;
     ismc_tune t;
     uint32_t blocks;
-    // device-resident instances: the total is not known on the host, size
-    // chunks for a large batch unless the caller chose
-    rc = resolve_tune(ctx, tune, (uint64_t)1 << 40, &t, &blocks);
+    rc = resolve_tune(ctx, tune, &t, &blocks);
     if (rc) return rc;
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
-    return enqueue_pipeline(ctx, d_inst, n_inst, t, blocks, d_out, s);
+    // the caller's stream exactly as given (NULL = the legacy default stream),
+    // so the launch is ordered with the caller's own copies and events
+    return enqueue_pipeline(ctx, d_inst, n_inst, t, blocks, d_out, (cudaStream_t)stream);
 }
 
 static bool same_tune(const ismc_tune& a, const ismc_tune& b) {
@@ -271,14 +267,14 @@ extern "C" int ismc_run_batch(ismc_ctx* ctx, const ismc_instance* inst, uint32_t
     CK(cudaSetDevice(ctx->device));
     rc = ensure_capacity(ctx, n_inst);
     if (rc) return rc;
-    const uint64_t total = total_packets(inst, n_inst);
     ismc_tune t;
     uint32_t blocks;
-    rc = resolve_tune(ctx, tune, total, &t, &blocks);
+    rc = resolve_tune(ctx, tune, &t, &blocks);
     if (rc) return rc;
     memcpy(ctx->h_in, inst, sizeof(ismc_instance) * n_inst);
     // replay the captured pipeline when batch size and launch shape repeat
-    if (!(ctx->gexec && ctx->g_n == n_inst && same_tune(ctx->g_tune, t))) {
+    if (!(ctx->gexec && ctx->g_n == n_inst && same_tune(ctx->g_tune, t) &&
+          ctx->g_cpw == ctx->chunks_per_warp)) {
         if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -297,6 +293,7 @@ extern "C" int ismc_run_batch(ismc_ctx* ctx, const ismc_instance* inst, uint32_t
             return set_err(ctx, ISMC_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
         ctx->g_n = n_inst;
         ctx->g_tune = t;
+        ctx->g_cpw = ctx->chunks_per_warp;
     }
     CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -351,39 +348,44 @@ extern "C" int ismc_autotune(ismc_ctx* ctx, const ismc_instance* inst, uint32_t 
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     const uint32_t threads_c[] = {128, 256, 512};
+    const uint32_t cpw_c[] = {2, 8, 32};
     float best = 1e30f;
     ismc_tune best_t = ctx->tune;
+    uint32_t best_cpw = ctx->chunks_per_warp;
+    const uint32_t saved_cpw = ctx->chunks_per_warp;
     for (uint32_t th : threads_c) {
-        int bps = 0;
-        if (ismc_propagate_occupancy(th, &bps) != 0 || bps <= 0) continue;
-        const uint64_t warps = (uint64_t)ctx->sms * bps * (th / 32);
-        const uint64_t base = std::max<uint64_t>(32, ttotal / (warps * 8 + 1));
-        const uint64_t cand[] = {base / 4, base, base * 4};
-        for (uint64_t cc : cand) {
-            ismc_tune t{th, 0, (uint32_t)std::max<uint64_t>(32, std::min<uint64_t>(cc, 65536) / 32 * 32), 0};
+        for (uint32_t cpw : cpw_c) {
+            ismc_tune t{th, 0, 0, 0};
             ismc_tune r;
             uint32_t blocks;
-            if (resolve_tune(ctx, &t, ttotal, &r, &blocks)) continue;
+            if (resolve_tune(ctx, &t, &r, &blocks)) continue;
+            ctx->chunks_per_warp = cpw;
             float best_ms = 1e30f;
             for (int rep = 0; rep < 2; ++rep) {
                 CK(cudaEventRecord(e0, ctx->stream));
                 rc = enqueue_pipeline(ctx, ctx->d_in, n_inst, r, blocks, ctx->d_out, ctx->stream);
-                if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+                if (rc) {
+                    ctx->chunks_per_warp = saved_cpw;
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    return rc;
+                }
                 CK(cudaEventRecord(e1, ctx->stream));
                 CK(cudaEventSynchronize(e1));
                 float ms = 0;
                 CK(cudaEventElapsedTime(&ms, e0, e1));
                 best_ms = std::min(best_ms, ms);
             }
-            if (best_ms < best) { best = best_ms; best_t = t; best_t.chunk_packets = 0; }
+            if (best_ms < best) { best = best_ms; best_t = t; best_cpw = cpw; }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    // keep the chunk size relative to the workload: store the winning block
-    // size; chunk size is re-derived from the real batch size on each call
+    // keep the winning block size and chunks-per-warp; the chunk size itself is
+    // re-derived on the device from each batch's total packet count
     ctx->tune.block_threads = best_t.block_threads;
     ctx->tune.blocks_per_sm = 0;
+    ctx->chunks_per_warp = best_cpw;
     ctx->tuned = true;
     if (out) *out = ctx->tune;
     return 0;

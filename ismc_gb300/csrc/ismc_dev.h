@@ -58,25 +58,26 @@ struct DevRange {
 
 // Tally block in device memory: same layout as ismc_tally so it can be copied
 // back verbatim.  Counters are added with 64-bit integer atomics.
-static_assert(sizeof(ismc_tally) == 8 * 15 + 4 * 4, "ismc_tally layout");
+static_assert(sizeof(ismc_tally) == 8 * 16 + 4 * 4, "ismc_tally layout");
 
 struct PropParams {
     const DevInst* inst;
     const DevRange* range;
     const unsigned long long* chunk_prefix;   // n_inst + 1 entries
     ismc_tally* tally;
-    unsigned long long* queue_head;
+    unsigned long long* ctrl;                 // [0] queue head, [1] packets per chunk
     uint32_t n_inst;
-    uint32_t chunk_packets;
     uint32_t max_events;
-    uint32_t _pad;
 };
 
 // Host-callable launchers (defined in ismc_kernels.cu).
+//   chunk_override: packets per queue chunk, 0 = derive on the device from the
+//   batch's total packets so that every warp gets ~chunks_per_warp chunks.
 extern "C++" {
 int ismc_launch_prepare(const ismc_instance* d_in, uint32_t n_inst, DevInst* d_inst,
                         DevRange* d_range, unsigned long long* d_prefix, ismc_tally* d_out,
-                        uint32_t chunk_packets, unsigned long long* d_queue, void* stream);
+                        unsigned long long* d_ctrl, uint32_t chunk_override, uint32_t total_warps,
+                        uint32_t chunks_per_warp, void* stream);
 int ismc_launch_propagate(const PropParams& p, uint32_t blocks, uint32_t threads, void* stream);
 int ismc_propagate_occupancy(uint32_t threads, int* blocks_per_sm);
 }

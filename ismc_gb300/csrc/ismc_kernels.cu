@@ -18,7 +18,8 @@
 
 #define ISMC_FULL 0xFFFFFFFFu
 #define ISMC_MAX_THREADS 512
-#define ISMC_NACC 14          // per-slot counters: sum[5], sumsq[5], steps, events, reinc, capped
+#define ISMC_NACC 15          // per-slot counters: sum[5], sumsq[5], steps, events, reinc,
+                              // capped, trapped
 
 // ============================================================================
 // Float-float arithmetic (an unevaluated sum hi + lo of two floats) for the
@@ -94,8 +95,7 @@ __device__ __forceinline__ bool ismc_finite(double x) { return isfinite(x); }
 
 __global__ void ismc_prepare_kernel(const ismc_instance* __restrict__ in, uint32_t n_inst,
                                     DevInst* __restrict__ out, DevRange* __restrict__ range,
-                                    unsigned long long* __restrict__ prefix,
-                                    ismc_tally* __restrict__ tally, uint32_t chunk_packets) {
+                                    ismc_tally* __restrict__ tally) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_inst) return;
     const ismc_instance& I = in[i];
@@ -229,7 +229,7 @@ __global__ void ismc_prepare_kernel(const ismc_instance* __restrict__ in, uint32
     ismc_tally& T = tally[i];
     T.n = ok ? I.n_packets : 0ull;
     for (int k = 0; k < 5; ++k) { T.sum[k] = 0ull; T.sumsq[k] = 0ull; }
-    T.steps = T.events = T.reincidences = T.capped = 0ull;
+    T.steps = T.events = T.reincidences = T.capped = T.trapped = 0ull;
     T.scale_log2 = 32u;
     T.status = ok ? ISMC_OK : ISMC_ERR_INVALID_ARG;
     T.analytic_specular = spec;
@@ -237,19 +237,47 @@ __global__ void ismc_prepare_kernel(const ismc_instance* __restrict__ in, uint32
     const uint64_t cnt = ok ? I.n_packets : 0ull;
     range[i].offset = I.packet_offset;
     range[i].count = cnt;
-    prefix[i + 1] = (cnt + chunk_packets - 1) / chunk_packets;
 }
 
-// Inclusive scan of the per-instance chunk counts (one block), prefix[0] = 0,
-// and reset of the queue head.
-__global__ void __launch_bounds__(1024) ismc_scan_kernel(unsigned long long* prefix, uint32_t n,
-                                                         unsigned long long* queue) {
+// One block: choose the packets per queue chunk from the batch's total packet
+// count (so that each warp gets ~chunks_per_warp chunks and the tail stays
+// short), then the inclusive prefix of per-instance chunk counts, prefix[0]=0,
+// and reset of the queue head.  ctrl[0] = queue head, ctrl[1] = chunk size.
+__global__ void __launch_bounds__(1024) ismc_scan_kernel(unsigned long long* prefix,
+                                                         const DevRange* __restrict__ range,
+                                                         uint32_t n, unsigned long long* ctrl,
+                                                         uint32_t chunk_override,
+                                                         uint32_t total_warps,
+                                                         uint32_t chunks_per_warp) {
     __shared__ unsigned long long part[1024];
+    __shared__ unsigned long long chunk_s;
     const uint32_t t = threadIdx.x;
     const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
     const uint32_t b = t * per, e = min(n, b + per);
+    // total packets
     unsigned long long s = 0;
-    for (uint32_t i = b; i < e; ++i) s += prefix[i + 1];
+    for (uint32_t i = b; i < e; ++i) s += range[i].count;
+    part[t] = s;
+    __syncthreads();
+    for (uint32_t off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (t < off) part[t] += part[t + off];
+        __syncthreads();
+    }
+    if (t == 0) {
+        unsigned long long c = chunk_override;
+        if (c == 0) {
+            const unsigned long long want = (unsigned long long)total_warps * max(chunks_per_warp, 1u);
+            c = (part[0] + want - 1) / want;
+            c = (c + 31) / 32 * 32;
+            c = min(max(c, 32ull), 65536ull);
+        }
+        chunk_s = c;
+    }
+    __syncthreads();
+    const unsigned long long chunk = chunk_s;
+    // per-instance chunk counts and their inclusive scan
+    s = 0;
+    for (uint32_t i = b; i < e; ++i) s += (range[i].count + chunk - 1) / chunk;
     part[t] = s;
     __syncthreads();
     for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
@@ -259,8 +287,15 @@ __global__ void __launch_bounds__(1024) ismc_scan_kernel(unsigned long long* pre
         __syncthreads();
     }
     unsigned long long run = t ? part[t - 1] : 0ull;
-    for (uint32_t i = b; i < e; ++i) { run += prefix[i + 1]; prefix[i + 1] = run; }
-    if (t == 0) { prefix[0] = 0ull; *queue = 0ull; }
+    for (uint32_t i = b; i < e; ++i) {
+        run += (range[i].count + chunk - 1) / chunk;
+        prefix[i + 1] = run;
+    }
+    if (t == 0) {
+        prefix[0] = 0ull;
+        ctrl[0] = 0ull;
+        ctrl[1] = chunk;
+    }
 }
 
 // ============================================================================
@@ -307,6 +342,17 @@ __device__ __forceinline__ void ismc_load_slot(WarpSlots* ws, int s, const DevIn
     constexpr int W = (int)(sizeof(DevInst) / 4);
     for (int k = lane; k < W; k += 32) d[k] = __ldg(g + k);
     __syncwarp();
+}
+
+// A packet inside slide l whose direction both faces totally reflect can never
+// leave.  In exact arithmetic refraction is reversible and this cannot happen;
+// in FP32 it can after near-grazing entry (|mu_z| ~ 1e-4 in the previous
+// layer).  Same expression as the TIR test of ismc_fresnel.
+__device__ __forceinline__ bool ismc_trapped(const DevInst& I, int l, float uz) {
+    const float ci = fabsf(uz);
+    const float s = 1.0f - ci * ci;
+    const float eu = I.eta_up[l], ed = I.eta_dn[l];
+    return (eu * eu) * s >= 1.0f && (ed * ed) * s >= 1.0f;
 }
 
 extern "C" __global__ void __launch_bounds__(ISMC_MAX_THREADS)
@@ -362,7 +408,7 @@ ismc_propagate_kernel(const PropParams P) {
             if (pend < 0) {
                 if (qdone) break;
                 unsigned long long c = 0;
-                if (lane == 0) c = atomicAdd(P.queue_head, 1ull);
+                if (lane == 0) c = atomicAdd(P.ctrl, 1ull);
                 c = __shfl_sync(ISMC_FULL, c, 0);
                 if (c >= n_chunks) { qdone = true; break; }
                 // instance owning chunk c: last i with prefix[i] <= c
@@ -376,9 +422,10 @@ ismc_propagate_kernel(const PropParams P) {
                     }
                     inst = (int)lo;
                     const DevRange R = P.range[lo];
+                    const unsigned long long chunk_packets = P.ctrl[1];
                     const unsigned long long j = c - P.chunk_prefix[lo];
-                    st = R.offset + j * P.chunk_packets;
-                    en = R.offset + min((unsigned long long)R.count, (j + 1) * P.chunk_packets);
+                    st = R.offset + j * chunk_packets;
+                    en = R.offset + min((unsigned long long)R.count, (j + 1) * chunk_packets);
                 }
                 pend = __shfl_sync(ISMC_FULL, inst, 0);
                 p_next = __shfl_sync(ISMC_FULL, st, 0);
@@ -418,7 +465,7 @@ ismc_propagate_kernel(const PropParams P) {
         const ismc_u4 r = ismc_philox4x32_10(ev, pk_lo, pk_hi, I.stream, I.seed_lo, I.seed_hi);
         ++ev;
         const float u0 = ismc_u01(r.x);
-        int fin = 0;          // 1: packet ended
+        int fin = 0;          // 1: packet ended, 2: event cap, 3: trapped in a slide
         int bin = -1;         // tally receiving the final weight
         bool to_sphere = false;
         float c_exit = 0.0f;  // |mu_z| of the packet entering a sphere
@@ -453,6 +500,7 @@ ismc_propagate_kernel(const PropParams P) {
                 layer = l;
                 phase = PH_WALK;
                 tau = (compat && (I.lflags[l] & ISMC_LF_GLASS)) ? 0.0f : ismc_neglog_u32(r.w);
+                if ((I.lflags[l] & ISMC_LF_GLASS) && ismc_trapped(I, l, uz)) fin = 3;
             }
         } else {
             // -------- walk inside layer l (MLMC.py:95-200)
@@ -494,6 +542,7 @@ ismc_propagate_kernel(const PropParams P) {
                     // interacts at the interface (MLMC.py:111, 148, 165-200)
                     if (compat && glass && !(I.lflags[nl] & ISMC_LF_GLASS)) tau = 0.0f;
                     layer = nl;
+                    if ((I.lflags[nl] & ISMC_LF_GLASS) && ismc_trapped(I, nl, uz)) fin = 3;
                 }
             } else {
                 // ---- interaction inside the layer: hop, drop, roulette, spin
@@ -570,13 +619,16 @@ ismc_propagate_kernel(const PropParams P) {
 
         if (fin) {
             unsigned long long* acc = ws->acc[slot];
-            if (fin == 1) {
+            if (fin != 2) {
+                // weight absorbed so far is scored; a trapped packet's
+                // remaining weight is dropped and counted
                 atomicAdd(acc + ISMC_T_A, ismc_q32(absorbed));
                 atomicAdd(acc + 5 + ISMC_T_A, ismc_q32(absorbed * absorbed));
                 if (bin >= 0) {
                     atomicAdd(acc + bin, ismc_q32(w));
                     atomicAdd(acc + 5 + bin, ismc_q32(w * w));
                 }
+                if (fin == 3) atomicAdd(acc + 14, 1ull);
             } else {
                 atomicAdd(acc + 13, 1ull);
                 atomicMin(&P.tally[slot ? s_inst1 : s_inst0].status, ISMC_ERR_STEP_LIMIT);
@@ -597,14 +649,16 @@ ismc_propagate_kernel(const PropParams P) {
 // ============================================================================
 int ismc_launch_prepare(const ismc_instance* d_in, uint32_t n_inst, DevInst* d_inst,
                         DevRange* d_range, unsigned long long* d_prefix, ismc_tally* d_out,
-                        uint32_t chunk_packets, unsigned long long* d_queue, void* stream) {
+                        unsigned long long* d_ctrl, uint32_t chunk_override, uint32_t total_warps,
+                        uint32_t chunks_per_warp, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     if (n_inst) {
         const uint32_t tb = 128;
         ismc_prepare_kernel<<<(n_inst + tb - 1) / tb, tb, 0, s>>>(d_in, n_inst, d_inst, d_range,
-                                                                 d_prefix, d_out, chunk_packets);
+                                                                 d_out);
     }
-    ismc_scan_kernel<<<1, 1024, 0, s>>>(d_prefix, n_inst, d_queue);
+    ismc_scan_kernel<<<1, 1024, 0, s>>>(d_prefix, d_range, n_inst, d_ctrl, chunk_override,
+                                        total_warps, chunks_per_warp);
     return cudaGetLastError() == cudaSuccess ? 0 : ISMC_ERR_CUDA;
 }
 

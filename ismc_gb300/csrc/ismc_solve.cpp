@@ -1,0 +1,202 @@
+// ismc_solve.cpp -- batched plain-path inverse solver over the C ABI.
+//
+// Each solve is a PRAXIS coroutine (ismc_praxis.h).  The driver resumes every
+// active solve until it asks for an objective value, turns all requests of the
+// round into one batch of Monte Carlo instances (1-3 per request), runs them
+// with ONE ismc_run_batch launch, scores the reference's cost and resumes.
+// Reference: minimization.py:201-271 (cost, Powell minimise, accept box with
+// retry), CUDA/ISMLMC-minimization.cu:89-131 (cost) and :466-488 (PRAXIS runs
+// with reject-and-retry, which is unbounded there and bounded here).
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "../../include/ismc.h"
+#include "ismc_praxis.h"
+
+using ismc::Praxis;
+using ismc::Task;
+
+namespace {
+
+enum SimKind { SIM_BOTH = 0, SIM_R = 1, SIM_T = 2, SIM_NONE = 3 };
+
+struct Solve {
+    const ismc_solve_req* req = nullptr;
+    Praxis px;
+    std::unique_ptr<Task<int>> task;
+    uint32_t evals = 0, restarts = 0, rounds = 0;
+    bool finished = false;
+    double best_cost = 0;
+    int32_t status = ISMC_OK;
+    // instances of the pending request
+    int first = -1, count = 0;
+    SimKind kinds[3];
+};
+
+inline double to_param(const ismc_solve_req& r, double u) { return r.log_coords ? std::exp(u) : u; }
+inline double from_param(const ismc_solve_req& r, double v) { return r.log_coords ? std::log(v) : v; }
+
+void start(Solve& s, uint32_t index, uint32_t attempt) {
+    const ismc_solve_req& r = *s.req;
+    s.px = Praxis();
+    s.px.n = 2;
+    s.px.t0 = r.t0;
+    s.px.h0 = r.h0;
+    s.px.maxfun = r.max_evals ? (int)r.max_evals : 2000;
+    s.px.rng = 0x243F6A8885A308D3ull ^ ((uint64_t)index << 20) ^ attempt;
+    s.px.x[0] = from_param(r, r.x0[0]);
+    s.px.x[1] = from_param(r, r.x0[1]);
+    s.task = std::make_unique<Task<int>>(ismc::praxis_run(s.px));
+    s.task->h.resume();   // runs to the first objective request
+}
+
+// The objective's Monte Carlo instances for the point p of solve s.
+int build_request(Solve& s, uint32_t index, const double* p, std::vector<ismc_instance>& out) {
+    const ismc_solve_req& r = *s.req;
+    const double mua = to_param(r, p[0]), musr = to_param(r, p[1]);
+    s.first = (int)out.size();
+    s.count = 0;
+    if (!(mua > 0) || !(musr > 0) || !std::isfinite(mua) || !std::isfinite(musr)) return 0;
+    ismc_instance base = r.base;
+    const uint32_t l = r.layer;
+    const double g = base.stack.g[l];
+    const double mus = g == 1.0 ? musr : musr / (1.0 - g);     // minimization.py:204-205
+    base.stack.mua[l] = (float)mua;
+    base.stack.mus[l] = (float)mus;
+    base.stack.mut[l] = (float)(mua + mus);
+    // independent Philox stream per (solve, evaluation, run kind)
+    const uint32_t ev = s.evals;
+    auto push = [&](SimKind k, bool R, bool T) {
+        ismc_instance x = base;
+        x.spheres.R = R ? 1 : 0;
+        x.spheres.T = T ? 1 : 0;
+        const uint32_t evk = r.fresh_streams ? ev : 0u;
+        x.stream = (uint32_t)(index * 2654435761u) ^ (evk << 2) ^ (uint32_t)k;
+        x.seed = r.base.seed + ((uint64_t)s.restarts << 40);
+        out.push_back(x);
+        s.kinds[s.count++] = k;
+    };
+    const bool hasRd = !std::isnan(r.meas[0]), hasRs = !std::isnan(r.meas[1]),
+               hasTd = !std::isnan(r.meas[2]), hasTu = !std::isnan(r.meas[3]);
+    if (r.separate) {
+        if (hasRd) push(SIM_R, true, false);
+        if (hasTd) push(SIM_T, false, true);
+        if (hasRs || hasTu) push(SIM_NONE, false, false);
+    } else {
+        push(SIM_BOTH, base.spheres.R != 0, base.spheres.T != 0);
+    }
+    return s.count;
+}
+
+double tally_mean(const ismc_tally& t, int k) {
+    return t.n ? (double)t.sum[k] / std::ldexp((double)t.n, (int)t.scale_log2) : NAN;
+}
+
+// minimization.py:231-238
+double score(const Solve& s, const ismc_tally* t) {
+    const ismc_solve_req& r = *s.req;
+    double Rd = NAN, Rs = NAN, Td = NAN, Tu = NAN;
+    for (int i = 0; i < s.count; ++i) {
+        const ismc_tally& x = t[s.first + i];
+        switch (s.kinds[i]) {
+            case SIM_BOTH: Rd = tally_mean(x, ISMC_T_RD); Rs = tally_mean(x, ISMC_T_RS);
+                           Td = tally_mean(x, ISMC_T_TD); Tu = tally_mean(x, ISMC_T_TU); break;
+            case SIM_R: Rd = tally_mean(x, ISMC_T_RD); break;
+            case SIM_T: Td = tally_mean(x, ISMC_T_TD); break;
+            case SIM_NONE: Rs = tally_mean(x, ISMC_T_RS); Tu = tally_mean(x, ISMC_T_TU); break;
+        }
+    }
+    double c = 0;
+    if (!std::isnan(r.meas[0])) c += std::pow((Rd - r.meas[0]) / r.meas[0], 2);
+    if (!std::isnan(r.meas[1])) c += std::pow(Rs - r.meas[1], 2);
+    if (!std::isnan(r.meas[2])) c += std::pow((Td - r.meas[2]) / r.meas[2], 2);
+    if (!std::isnan(r.meas[3])) c += std::pow(Tu - r.meas[3], 2);
+    return std::isfinite(c) ? std::sqrt(c) : 1e30;
+}
+
+}  // namespace
+
+extern "C" int ismc_praxis(ismc_objective f, void* user, int n, double* x, double t0, double h0,
+                           int maxfun, double* fmin, int* nevals) {
+    if (!f || !x || n < 1 || n > ismc::PRAXIS_NMAX || !(h0 > 0)) return ISMC_ERR_INVALID_ARG;
+    double v = ismc::praxis_minimize(f, user, n, x, t0, h0, maxfun > 0 ? maxfun : 2000, nevals);
+    if (fmin) *fmin = v;
+    return ISMC_OK;
+}
+
+extern "C" int ismc_solve_batch(ismc_ctx* ctx, const ismc_solve_req* req, uint32_t n,
+                                ismc_solve_out* out) {
+    if (!ctx || !req || !out || n == 0) return ISMC_ERR_INVALID_ARG;
+    for (uint32_t i = 0; i < n; ++i) {
+        const ismc_solve_req& r = req[i];
+        if (r.layer >= r.base.stack.L || r.base.stack.L > ISMC_MAXL || !(r.h0 > 0) ||
+            !(r.x0[0] > 0) || !(r.x0[1] > 0) || r.base.n_packets == 0)
+            return ISMC_ERR_INVALID_ARG;
+    }
+    std::vector<Solve> S(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        S[i].req = &req[i];
+        start(S[i], i, 0);
+    }
+    std::vector<ismc_instance> batch;
+    std::vector<ismc_tally> tallies;
+    std::vector<uint32_t> active;
+    for (;;) {
+        batch.clear();
+        active.clear();
+        for (uint32_t i = 0; i < n; ++i) {
+            Solve& s = S[i];
+            for (;;) {
+                if (!s.finished && s.task->h.done()) {
+                    // a minimisation ended: accept, or restart when outside the box
+                    const ismc_solve_req& r = *s.req;
+                    const double a = to_param(r, s.px.x[0]), b = to_param(r, s.px.x[1]);
+                    const bool inside =
+                        a >= r.lo[0] && a <= r.hi[0] && b >= r.lo[1] && b <= r.hi[1];
+                    if (inside || s.restarts >= r.max_restarts) {
+                        s.finished = true;
+                        s.status = inside ? ISMC_OK : ISMC_ERR_CAPACITY;
+                        out[i].x[0] = a;
+                        out[i].x[1] = b;
+                        out[i].cost = s.px.fx;
+                    } else {
+                        ++s.restarts;
+                        start(s, i, s.restarts);
+                    }
+                    continue;
+                }
+                if (s.finished) break;
+                if (build_request(s, i, s.px.point, batch) == 0) {
+                    // outside the physical domain: infinite cost, no simulation
+                    s.px.value = 1e30;
+                    ++s.evals;
+                    s.px.waiting.resume();
+                    continue;
+                }
+                active.push_back(i);
+                break;
+            }
+        }
+        if (active.empty()) break;
+        tallies.resize(batch.size());
+        const int rc = ismc_run_batch(ctx, batch.data(), (uint32_t)batch.size(), nullptr,
+                                      tallies.data());
+        if (rc) return rc;
+        for (uint32_t i : active) {
+            Solve& s = S[i];
+            s.px.value = score(s, tallies.data());
+            ++s.evals;
+            ++s.rounds;
+            s.px.waiting.resume();
+        }
+    }
+    for (uint32_t i = 0; i < n; ++i) {
+        out[i].evals = S[i].evals;
+        out[i].restarts = S[i].restarts;
+        out[i].status = S[i].status;
+        out[i].rounds = S[i].rounds;
+    }
+    return ISMC_OK;
+}

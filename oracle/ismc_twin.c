@@ -178,11 +178,20 @@ static void prepare(const ismc_instance* I, TwinInst* D) {
     D->eta_in[1] = 1.0f / S->n[L - 1];
 }
 
+/* A slide that totally reflects the direction on both faces cannot be left;
+ * only rounding at near-grazing entry produces this.  Same test as fresnel(). */
+static int trapped_in(const TwinInst* I, int l, float uz) {
+    const float ci = fabsf(uz);
+    const float s = 1.0f - ci * ci;
+    const float eu = I->eta_up[l], ed = I->eta_dn[l];
+    return (eu * eu) * s >= 1.0f && (ed * ed) * s >= 1.0f;
+}
+
 /* ------------------------------------------------------------ one packet */
 typedef struct {
     float absorbed, w;
     int bin;            /* tally of the final weight, -1 none */
-    int capped;
+    int capped, trapped;
     uint32_t steps, events, reinc;
 } TwinPacket;
 
@@ -229,6 +238,7 @@ static void run_packet(const TwinInst* I, uint64_t id, uint32_t max_events, Twin
                 layer = l;
                 incident = 0;
                 tau = (compat && I->glass[l]) ? 0.0f : neglog_u32(r[3]);
+                if (I->glass[l] && trapped_in(I, l, uz)) fin = 3;
             }
         } else {
             /* walk (MLMC.py:95-200) */
@@ -267,6 +277,7 @@ static void run_packet(const TwinInst* I, uint64_t id, uint32_t max_events, Twin
                     inv_uz = 1.0f / uz;
                     if (compat && glass && !I->glass[nl]) tau = 0.0f;
                     layer = nl;
+                    if (I->glass[nl] && trapped_in(I, nl, uz)) fin = 3;
                 }
             } else {
                 const float s = tau * I->inv_mut[l];
@@ -339,6 +350,7 @@ static void run_packet(const TwinInst* I, uint64_t id, uint32_t max_events, Twin
     o->w = w;
     o->bin = fin == 1 ? bin : -1;
     o->capped = fin == 2;
+    o->trapped = fin == 3;
     o->steps = steps;
     o->events = ev;
     o->reinc = reinc;
@@ -362,6 +374,7 @@ static void add_packet(ismc_tally* t, const TwinPacket* p) {
             t->sum[p->bin] += q32(p->w);
             t->sumsq[p->bin] += q32(p->w * p->w);
         }
+        if (p->trapped) t->trapped += 1;
     }
     t->steps += p->steps;
     t->events += p->events;
@@ -405,6 +418,7 @@ int twin_run(const ismc_instance* inst, uint32_t max_events, int threads, ismc_t
         out->events += w[k].t.events;
         out->reincidences += w[k].t.reincidences;
         out->capped += w[k].t.capped;
+        out->trapped += w[k].t.trapped;
     }
     out->n = n;
     out->scale_log2 = 32;

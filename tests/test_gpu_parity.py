@@ -31,7 +31,8 @@ ANALYTIC_RTOL = 1e-6
 
 def _same(a, b):
     return (list(a.sum) == list(b.sum) and list(a.sumsq) == list(b.sumsq) and a.steps == b.steps
-            and a.events == b.events and a.reincidences == b.reincidences and a.capped == b.capped)
+            and a.events == b.events and a.reincidences == b.reincidences and a.capped == b.capped
+            and a.trapped == b.trapped)
 
 
 def _diff(a, b):
