@@ -183,6 +183,30 @@ int ismc_run_batch(ismc_ctx* ctx, const ismc_instance* inst, uint32_t n_inst,
 int ismc_run_batch_device(ismc_ctx* ctx, const ismc_instance* d_inst, uint32_t n_inst,
                           const ismc_tune* tune, ismc_tally* d_out, void* stream);
 
+/*
+ * Batch entry point that allocates no GPU memory (no counterpart in the
+ * reference, which allocates and frees on every call).  For callers that may
+ * not call cudaMalloc: a plugin inside an application that owns all device
+ * memory, a fixed memory budget, or a loop that cannot take an allocation's
+ * implicit synchronisation.  Inputs and outputs are the caller's device
+ * pointers, as for ismc_run_batch_device; the library's working memory is one
+ * fixed __device__ array sized for ISMC_NOALLOC_MAX_INST instances (~1 MB,
+ * kept by every GPU that loads the library until the process exits).
+ *   - Needs no context; runs on the calling thread's current device and on
+ *     `stream` as given (NULL = legacy default stream).
+ *   - The first call on a device looks up the array's device address; make
+ *     that first call before any stream capture.
+ *   - n_inst > ISMC_NOALLOC_MAX_INST returns ISMC_ERR_CAPACITY (message in
+ *     ismc_last_error(NULL, ...)).
+ *   - All calls share the one array: calls that overlap on the GPU (different
+ *     streams, or different host threads) race and corrupt each other.
+ *     Serialise them, e.g. on one stream.  Each call re-initialises everything
+ *     it reads, so results never depend on an earlier call.
+ */
+#define ISMC_NOALLOC_MAX_INST 1024
+int ismc_run_batch_noalloc(const ismc_instance* d_inst, uint32_t n_inst, const ismc_tune* tune,
+                           ismc_tally* d_out, void* stream);
+
 /* Choose block size / chunk size for a representative batch by timing short
  * trial launches; the choice is stored in the context and returned in *out. */
 int ismc_autotune(ismc_ctx* ctx, const ismc_instance* inst, uint32_t n_inst,

@@ -81,7 +81,9 @@ SIZEOF_INDEX = {0: Stack, 1: Spheres, 2: Instance, 3: Tally, 4: Tune, 5: SolveRe
 # every symbol include/ismc.h declares
 EXPORTS = ("ismc_version", "ismc_init", "ismc_destroy", "ismc_run", "ismc_run_batch",
            "ismc_run_batch_device", "ismc_autotune", "ismc_last_error", "ismc_sizeof",
-           "ismc_solve_batch", "ismc_praxis")
+           "ismc_solve_batch", "ismc_praxis", "ismc_run_batch_noalloc")
+
+NOALLOC_MAX_INST = 1024
 
 
 def declare(lib):
@@ -110,6 +112,8 @@ def declare(lib):
     lib.ismc_praxis.restype = C.c_int
     lib.ismc_praxis.argtypes = [OBJECTIVE, C.c_void_p, C.c_int, P(C.c_double), C.c_double,
                                 C.c_double, C.c_int, P(C.c_double), P(C.c_int)]
+    lib.ismc_run_batch_noalloc.restype = C.c_int
+    lib.ismc_run_batch_noalloc.argtypes = [C.c_void_p, C.c_uint32, P(Tune), C.c_void_p, C.c_void_p]
     lib.ismc_sizeof.restype = C.c_size_t
     lib.ismc_sizeof.argtypes = [C.c_int]
     for k, cls in SIZEOF_INDEX.items():

@@ -54,6 +54,14 @@ static int set_err(ismc_ctx* c, int code, const char* fmt, ...) {
     return code;
 }
 
+int ismc_lib_error(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_lib_err, sizeof(g_lib_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
 #define CK(call)                                                                         \
     do {                                                                                 \
         cudaError_t e_ = (call);                                                         \

@@ -80,4 +80,6 @@ int ismc_launch_prepare(const ismc_instance* d_in, uint32_t n_inst, DevInst* d_i
                         uint32_t chunks_per_warp, void* stream);
 int ismc_launch_propagate(const PropParams& p, uint32_t blocks, uint32_t threads, void* stream);
 int ismc_propagate_occupancy(uint32_t threads, int* blocks_per_sm);
+// Record a library-level error (no context): text for ismc_last_error(NULL).
+int ismc_lib_error(int code, const char* fmt, ...);
 }
