@@ -259,6 +259,33 @@ typedef double (*ismc_objective)(const double* x, int n, void* user);
 int ismc_praxis(ismc_objective f, void* user, int n, double* x, double t0, double h0,
                 int maxfun, double* fmin, int* nevals);
 
+/* ------------------------------------------------------------------------
+ * Surrogate network (no counterpart in the reference): MLP
+ * 5 -> 256 -> 256 -> 256 -> 6, SiLU, BF16 weights/activations, FP32
+ * accumulation on the tcgen05 tensor cores, Adam, Gaussian negative
+ * log-likelihood.  Inputs per row: (ln mu_a, ln mu_s', g, d, n), mapped
+ * internally from [ln .01, ln 10] x [ln 1, ln 100] x [.6, .95] x [.02, .5] x
+ * [1.33, 1.5] to [-1, 1]; outputs per row: means of (R_d, T_d, T_u) and their
+ * log-variances.  All array arguments are DEVICE pointers, row-major fp32;
+ * batch sizes are multiples of 128.  Parameters are flattened as
+ * W1[256x5], b1, W2[256x256], b2, W3[256x256], b3, W4[6x256], b4.
+ * ------------------------------------------------------------------------ */
+typedef struct ismc_mlp ismc_mlp;
+int ismc_mlp_create(int device, uint32_t max_batch, uint64_t seed, ismc_mlp** out);
+int ismc_mlp_destroy(ismc_mlp* m);
+size_t ismc_mlp_nparam(void);
+int ismc_mlp_get_params(ismc_mlp* m, float* host, size_t n);        /* host array */
+int ismc_mlp_set_params(ismc_mlp* m, const float* host, size_t n);  /* resets Adam */
+int ismc_mlp_forward(ismc_mlp* m, const float* d_x, uint32_t batch, float* d_out);
+int ismc_mlp_grad(ismc_mlp* m, const float* d_x, const float* d_y, uint32_t batch,
+                  float* d_grad, float* loss /* host, may be NULL */);
+int ismc_mlp_train_step(ismc_mlp* m, const float* d_x, const float* d_y, uint32_t batch,
+                        float lr, float* loss /* host; NULL = do not wait */);
+int ismc_mlp_sync(ismc_mlp* m);
+int ismc_mlp_gemm_test(ismc_mlp* m, const void* d_a, const void* d_b, float* d_d, int M, int N,
+                       int K, int splits);   /* D = A B^T, bf16 K-major operands, for tests */
+int ismc_mlp_last_error(const ismc_mlp* m, char* buf, size_t n);
+
 /* Sizes of the ABI structs, so bindings can check their own layouts. */
 size_t ismc_sizeof(int which);   /* 0 stack, 1 spheres, 2 instance, 3 tally, 4 tune,
                                     5 solve_req, 6 solve_out */

@@ -81,7 +81,10 @@ SIZEOF_INDEX = {0: Stack, 1: Spheres, 2: Instance, 3: Tally, 4: Tune, 5: SolveRe
 # every symbol include/ismc.h declares
 EXPORTS = ("ismc_version", "ismc_init", "ismc_destroy", "ismc_run", "ismc_run_batch",
            "ismc_run_batch_device", "ismc_autotune", "ismc_last_error", "ismc_sizeof",
-           "ismc_solve_batch", "ismc_praxis", "ismc_run_batch_noalloc")
+           "ismc_solve_batch", "ismc_praxis", "ismc_run_batch_noalloc",
+           "ismc_mlp_create", "ismc_mlp_destroy", "ismc_mlp_nparam", "ismc_mlp_get_params",
+           "ismc_mlp_set_params", "ismc_mlp_forward", "ismc_mlp_grad", "ismc_mlp_train_step",
+           "ismc_mlp_sync", "ismc_mlp_gemm_test", "ismc_mlp_last_error")
 
 NOALLOC_MAX_INST = 1024
 
@@ -114,6 +117,29 @@ def declare(lib):
                                 C.c_double, C.c_int, P(C.c_double), P(C.c_int)]
     lib.ismc_run_batch_noalloc.restype = C.c_int
     lib.ismc_run_batch_noalloc.argtypes = [C.c_void_p, C.c_uint32, P(Tune), C.c_void_p, C.c_void_p]
+    V, F = C.c_void_p, P(C.c_float)
+    lib.ismc_mlp_create.restype = C.c_int
+    lib.ismc_mlp_create.argtypes = [C.c_int, C.c_uint32, C.c_uint64, P(V)]
+    lib.ismc_mlp_destroy.restype = C.c_int
+    lib.ismc_mlp_destroy.argtypes = [V]
+    lib.ismc_mlp_nparam.restype = C.c_size_t
+    lib.ismc_mlp_nparam.argtypes = []
+    lib.ismc_mlp_get_params.restype = C.c_int
+    lib.ismc_mlp_get_params.argtypes = [V, F, C.c_size_t]
+    lib.ismc_mlp_set_params.restype = C.c_int
+    lib.ismc_mlp_set_params.argtypes = [V, F, C.c_size_t]
+    lib.ismc_mlp_forward.restype = C.c_int
+    lib.ismc_mlp_forward.argtypes = [V, V, C.c_uint32, V]
+    lib.ismc_mlp_grad.restype = C.c_int
+    lib.ismc_mlp_grad.argtypes = [V, V, V, C.c_uint32, V, F]
+    lib.ismc_mlp_train_step.restype = C.c_int
+    lib.ismc_mlp_train_step.argtypes = [V, V, V, C.c_uint32, C.c_float, F]
+    lib.ismc_mlp_sync.restype = C.c_int
+    lib.ismc_mlp_sync.argtypes = [V]
+    lib.ismc_mlp_gemm_test.restype = C.c_int
+    lib.ismc_mlp_gemm_test.argtypes = [V, V, V, V, C.c_int, C.c_int, C.c_int, C.c_int]
+    lib.ismc_mlp_last_error.restype = C.c_int
+    lib.ismc_mlp_last_error.argtypes = [V, C.c_char_p, C.c_size_t]
     lib.ismc_sizeof.restype = C.c_size_t
     lib.ismc_sizeof.argtypes = [C.c_int]
     for k, cls in SIZEOF_INDEX.items():

@@ -1,0 +1,122 @@
+"""Workload runners of the benchmark set beyond the headline forward run
+(used by `bench.py --workload ...`).
+
+  lookup     batched lookup-table generation: 64 x 64 single-slab grid with
+             photon budgets log-uniform over 1e5-1e7 plus 512 random 1-5 layer
+             stacks, all in one persistent launch (photons/s)
+  surrogate  training data from batched Monte Carlo + training of the MLP on
+             the tensor cores (samples/s of data generation, training steps/s,
+             held-out error against high-count Monte Carlo)
+  solve      batched inverse solve: plain path (PRAXIS on Monte Carlo) against
+             the surrogate-assisted path (solves/s, error vs truth, fallbacks)
+
+All inputs are synthetic and seeded; sizes scale with `scale` so the same code
+runs as a quick check or at the full sizes of the benchmark set.
+"""
+import math
+import time
+
+import numpy as np
+
+from .api import Engine, make_solve, tally_to_result
+from .workloads import bench_spheres, lookup_grid
+
+
+def run_lookup(engine: Engine, scale=1.0, seed=2, tune=None):
+    insts = lookup_grid(seed=seed, scale=scale)
+    n_packets = sum(int(x.n_packets) for x in insts)
+    engine.run_batch(insts[:64], tune)           # warm the graph/caches on a small slice
+    t0 = time.perf_counter()
+    raw = engine.run_batch_raw(insts, tune)
+    dt = time.perf_counter() - t0
+    res = [tally_to_result(t) for t in raw]
+    steps = sum(r.steps for r in res)
+    return {"instances": len(insts), "packets": n_packets, "seconds": dt,
+            "photons_per_s": n_packets / dt, "steps_per_s": steps / dt,
+            "steps_per_packet": steps / n_packets,
+            "statuses_ok": all(r.status == 0 for r in res)}
+
+
+def make_measurements(engine, n, seed=4, packets=1_000_000, g=0.9, d=0.1, nidx=1.4,
+                      noise=(0.002, 0.002, 0.0005)):
+    """Synthetic measurements: MC at true (mu_a, mu_s') log-uniform over the
+    surrogate's ranges, plus Gaussian noise on (R_d, T_d, T_u)."""
+    from .surrogate import simulate
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lmua = rng.uniform(math.log(0.01), math.log(10.0), n)
+    lmus = rng.uniform(math.log(1.0), math.log(100.0), n)
+    X = np.stack([lmua, lmus, np.full(n, g), np.full(n, d), np.full(n, nidx)], 1)
+    Y, _ = simulate(engine, X, packets, seed=seed + 1000)
+    Yn = Y + rng.standard_normal(Y.shape) * np.asarray(noise)
+    return np.exp(X[:, :2]), Yn
+
+
+def run_surrogate(engine, n_samples=1 << 20, packets=100_000, epochs=20, batch=4096, seed=42,
+                  heldout=32, heldout_packets=10_000_000):
+    """Generate training data with the batched MC, train on the tensor cores,
+    score on a held-out (mu_a, mu_s', g) grid at d = 0.1 cm, n = 1.4."""
+    from .surrogate import LO, HI, Surrogate, sample_inputs, simulate
+    X = sample_inputs(n_samples, seed=seed)
+    t0 = time.perf_counter()
+    Y, S = simulate(engine, X, packets, seed=seed)
+    t_gen = time.perf_counter() - t0
+    sur = Surrogate(0, max_batch=batch, seed=seed)
+    t1 = time.perf_counter()
+    hist = sur.train(X.astype(np.float32), Y.astype(np.float32), epochs=epochs, batch=batch,
+                     lr=1e-3, seed=seed)
+    t_train = time.perf_counter() - t1
+    steps = epochs * (n_samples // batch)
+    # held-out grid
+    a = np.linspace(LO[0], HI[0], heldout)
+    s = np.linspace(LO[1], HI[1], heldout)
+    gg = np.linspace(LO[2], HI[2], heldout)
+    A, Sg, G = np.meshgrid(a, s, gg, indexing="ij")
+    Xh = np.stack([A.ravel(), Sg.ravel(), G.ravel(), np.full(A.size, 0.1), np.full(A.size, 1.4)], 1)
+    Yh, Sh = simulate(engine, Xh, heldout_packets, seed=seed + 7)
+    P = sur.forward(Xh.astype(np.float32)).cpu().numpy()[:, :3]
+    err = np.abs(P - Yh)
+    out = {"samples": n_samples, "packets_per_sample": packets, "datagen_s": t_gen,
+           "datagen_samples_per_s": n_samples / t_gen, "train_s": t_train,
+           "train_steps": steps, "train_steps_per_s": steps / t_train, "loss_history": hist,
+           "heldout_points": len(Xh), "heldout_packets": heldout_packets,
+           "heldout_mae": err.mean(0).tolist(), "heldout_rmse": np.sqrt((err ** 2).mean(0)).tolist(),
+           "heldout_max": err.max(0).tolist(), "heldout_mc_se_mean": Sh.mean(0).tolist()}
+    return sur, out
+
+
+def run_solve(engine, sur, n_meas=10000, n_plain=200, seed=4, verify_packets=1_000_000,
+              plain_packets=100_000):
+    """Plain path on a subsample and surrogate-assisted path on all measurements."""
+    from .surrogate import sample_stack, surrogate_solve
+    truth, meas = make_measurements(engine, n_meas, seed=seed)
+    sig = np.array([0.002, 0.002, 0.0005])
+    sph = bench_spheres()
+    # plain path: PRAXIS + 1e5-packet MC objective, batched across solves
+    k = min(n_plain, n_meas)
+    reqs = [make_solve(sample_stack(1.0, 10.0, 0.9, 0.1, 1.4), 1, sph, plain_packets,
+                       (meas[i, 0], None, meas[i, 1], meas[i, 2]), x0=(0.3, 10.0), seed=seed + i,
+                       max_evals=400) for i in range(k)]
+    t0 = time.perf_counter()
+    outp = engine.solve_batch(reqs)
+    t_plain = time.perf_counter() - t0
+    xp = np.array([[o.x[0], o.x[1]] for o in outp])
+    ev = np.array([o.evals for o in outp])
+    # surrogate path on every measurement
+    t1 = time.perf_counter()
+    rs = surrogate_solve(sur, engine, meas, sig, verify_packets=verify_packets,
+                         plain_packets=plain_packets, seed=seed + 99)
+    t_sur = time.perf_counter() - t1
+    xs = rs["x"]
+
+    def rel(x, t):
+        e = np.abs(x / t - 1)
+        return {"median": np.median(e, 0).tolist(), "p90": np.percentile(e, 90, 0).tolist()}
+
+    return {"measurements": n_meas, "plain_subsample": k,
+            "plain_solves_per_s": k / t_plain, "plain_evals_mean": float(ev.mean()),
+            "plain_rel_err_vs_truth": rel(xp, truth[:k]),
+            "surrogate_solves_per_s": n_meas / t_sur,
+            "surrogate_rel_err_vs_truth": rel(xs, truth),
+            "surrogate_vs_plain_rel_diff": rel(xs[:k], xp),
+            "fallback_rate": float(rs["fallback"].mean()), "surrogate_timing": rs["timing"],
+            "speedup": (n_meas / t_sur) / (k / t_plain)}

@@ -24,8 +24,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + os.path.join(ROOT, "include")] + ARCH
 
-SOURCES = ["ismc_kernels.cu", "ismc_capi.cu", "ismc_noalloc.cu", "ismc_praxis.cpp",
-           "ismc_solve.cpp"]
+SOURCES = ["ismc_kernels.cu", "ismc_capi.cu", "ismc_noalloc.cu", "ismc_mlp.cu",
+           "ismc_praxis.cpp", "ismc_solve.cpp"]
 CXX_FLAGS = ["-O2", "-std=c++20", "-fPIC", "-ffp-contract=off", "-Wall",
              "-I" + os.path.join(ROOT, "include")]
 

@@ -364,7 +364,6 @@ ismc_propagate_kernel(const PropParams P) {
     __syncwarp();
     const unsigned long long n_chunks = P.chunk_prefix[P.n_inst];
     const unsigned lt_mask = (1u << lane) - 1u;
-    const float INF = __int_as_float(0x7f800000);
 
     // ---- warp-uniform queue state
     int s_inst0 = -1, s_inst1 = -1;      // instance held by slot 0 / 1
@@ -379,7 +378,7 @@ ismc_propagate_kernel(const PropParams P) {
     int slot = 0, layer = 0;
     uint32_t phase = PH_INCIDENT, side = 0;     // side 0 = R (top), 1 = T (bottom)
     uint32_t ev = 0, pk_lo = 0, pk_hi = 0, steps = 0, reinc = 0;
-    float w = 0.f, z = 0.f, ux = 0.f, uy = 0.f, uz = 1.f, inv_uz = 1.f, tau = 0.f, absorbed = 0.f;
+    float w = 0.f, z = 0.f, ux = 0.f, uy = 0.f, uz = 1.f, tau = 0.f, absorbed = 0.f;
 
     for (;;) {
         // ================================================= hand out packets
@@ -399,7 +398,7 @@ ismc_propagate_kernel(const PropParams P) {
                     ev = 0; steps = 0; reinc = 0;
                     phase = PH_INCIDENT; side = 0;
                     w = 1.0f; absorbed = 0.0f; z = 0.0f; tau = 0.0f; layer = 0;
-                    ux = I.ux0; uy = 0.0f; uz = I.uz0; inv_uz = 1.0f;
+                    ux = I.ux0; uy = 0.0f; uz = I.uz0;
                 }
                 c_next += k;
                 need = __ballot_sync(ISMC_FULL, !alive);
@@ -495,7 +494,6 @@ ismc_propagate_kernel(const PropParams P) {
                 ux = ux * eta;
                 uy = uy * eta;
                 uz = top ? ct : -ct;
-                inv_uz = __frcp_rn(uz);
                 z = top ? 0.0f : I.t_tot;
                 layer = l;
                 phase = PH_WALK;
@@ -508,15 +506,19 @@ ismc_propagate_kernel(const PropParams P) {
             const bool down = uz > 0.0f;
             const bool glass = (I.lflags[l] & ISMC_LF_GLASS) != 0u;
             const float zb = down ? I.z_bot[l] : I.z_top[l];
-            const float d = (uz == 0.0f) ? INF : fmaxf((zb - z) * inv_uz, 0.0f);
+            // distance to the boundary along z (rounding can leave z a hair outside)
+            const float dist = fmaxf(down ? zb - z : z - zb, 0.0f);
+            const float auz = fabsf(uz);
             const float mut = I.mut[l];
-            if (glass && uz == 0.0f) {
+            if (glass && auz == 0.0f) {
                 fin = 2;                                   // cannot leave a slide: give up on it
-            } else if (glass || tau >= d * mut) {
-                // ---- reach the interface
+            } else if (glass || (auz > 0.0f && dist * mut <= tau * auz)) {
+                // ---- reach the interface (free path tau/mut >= dist/|uz|, no division)
                 if (!glass) {
+                    const float d = __fdiv_rn(dist, auz);
                     tau = fmaxf(__fmaf_rn(-d, mut, tau), 0.0f);
                 } else if (!compat && I.drop[l] > 0.0f) {
+                    const float d = __fdiv_rn(dist, auz);
                     const float wn = w * ismc_expneg(I.drop[l] * d);
                     absorbed = absorbed + (w - wn);
                     w = wn;
@@ -525,10 +527,9 @@ ismc_propagate_kernel(const PropParams P) {
                 const int nl = down ? l + 1 : l - 1;
                 const float eta = down ? I.eta_dn[l] : I.eta_up[l];
                 float ct;
-                const float R = ismc_fresnel(eta, fabsf(uz), &ct);
+                const float R = ismc_fresnel(eta, auz, &ct);
                 if (u0 < R) {
                     uz = -uz;
-                    inv_uz = -inv_uz;
                 } else if (nl < 0 || nl >= (int)L) {
                     side = nl < 0 ? 0u : 1u;
                     to_sphere = true;
@@ -537,7 +538,6 @@ ismc_propagate_kernel(const PropParams P) {
                     ux = ux * eta;
                     uy = uy * eta;
                     uz = down ? ct : -ct;
-                    inv_uz = __frcp_rn(uz);
                     // slide -> tissue leaves no path to spend: the packet
                     // interacts at the interface (MLMC.py:111, 148, 165-200)
                     if (compat && glass && !(I.lflags[nl] & ISMC_LF_GLASS)) tau = 0.0f;
@@ -568,25 +568,27 @@ ismc_propagate_kernel(const PropParams P) {
                     }
                     float sp, cp;
                     ismc_sincos_2pi(u2, &sp, &cp);
-                    const float sth = __fsqrt_rn(fmaxf(__fmaf_rn(-cth, cth, 1.0f), 0.0f));
+                    const float s2 = fmaxf(__fmaf_rn(-cth, cth, 1.0f), 0.0f);   // sin^2 theta
                     if (fabsf(uz) > 0.99999f) {             // MLMC.py:190-193
+                        const float sth = __fsqrt_rn(s2);
                         ux = sth * cp;
                         uy = sth * sp;
                         uz = uz > 0.0f ? cth : -cth;
                     } else {                                 // MLMC.py:194-198
-                        // sin of the polar angle from the transverse components:
-                        // equal to sqrt(1 - uz^2) for a unit vector, but keeps
-                        // the FP32 norm error from growing as 1/(1 - uz^2)
-                        const float zs = __fsqrt_rn(__fmaf_rn(ux, ux, uy * uy));
-                        const float k = __fdiv_rn(sth, zs);
+                        // rho2 = sin^2 of the polar angle from the transverse
+                        // components (= 1 - uz^2 for a unit vector; this form keeps
+                        // the FP32 norm error from growing as 1/(1 - uz^2)), and
+                        // k = sin(theta)/sin(polar) from one division and one root:
+                        //   new = k (ux uz cp - uy sp, uy uz cp + ux sp, -rho2 cp) + cth u
+                        const float rho2 = __fmaf_rn(ux, ux, uy * uy);
+                        const float k = __fsqrt_rn(__fdiv_rn(s2, rho2));
                         const float bx = __fmaf_rn(ux * uz, cp, -(uy * sp));
                         const float by = __fmaf_rn(uy * uz, cp, ux * sp);
                         const float nx = __fmaf_rn(k, bx, ux * cth);
                         const float ny = __fmaf_rn(k, by, uy * cth);
-                        const float nz = __fmaf_rn(-(sth * cp), zs, uz * cth);
+                        const float nz = __fmaf_rn(-(k * cp), rho2, uz * cth);
                         ux = nx; uy = ny; uz = nz;
                     }
-                    inv_uz = __frcp_rn(uz);
                     tau = ismc_neglog_u32(r.w);
                 }
             }

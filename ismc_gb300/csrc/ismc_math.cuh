@@ -46,22 +46,26 @@ __device__ __forceinline__ float ismc_u01(uint32_t x) {
 
 // -ln(u) for u in (0,1], from u = x * 2^-32 with x forced odd (32-bit
 // resolution keeps the exponential tail to 22.9 mean free paths).
-//   ln u = e ln2 + ln m,  m in (sqrt(1/2), sqrt(2)],
-//   ln m = 2 atanh(t) = 2 (t + t^3/3 + t^5/5 + t^7/7 + t^9/9 + ...), t = (m-1)/(m+1),
-// |t| <= 0.1716, so the series truncated after t^9 is accurate to 2e-9.
+//   ln u = e ln2 + ln m,  m in (sqrt(1/2), sqrt(2)],  f = m - 1 (exact),
+//   ln m = f - f^2/2 + f^3 Q(f),
+// Q a degree-7 least-squares polynomial (derivation and error check:
+// fit_log_poly.py; max relative error 1.3e-7).  No division.
 __device__ __forceinline__ float ismc_neglog_u32(uint32_t x) {
     const float u = __uint2float_rn(x | 1u) * 2.3283064365386963e-10f;  // 2^-32
     const uint32_t b = __float_as_uint(u);
     int e = (int)(b >> 23) - 127;
     float m = __uint_as_float((b & 0x007FFFFFu) | 0x3F800000u);
     if (m > 1.41421354f) { m = m * 0.5f; e += 1; }
-    const float t = __fdiv_rn(m - 1.0f, m + 1.0f);
-    const float t2 = t * t;
-    float p = __fmaf_rn(t2, 0.111111112f, 0.142857149f);   // 1/9, 1/7
-    p = __fmaf_rn(t2, p, 0.200000003f);                     // 1/5
-    p = __fmaf_rn(t2, p, 0.333333343f);                     // 1/3
-    p = __fmaf_rn(t2, p, 1.0f);
-    const float lnm = (2.0f * t) * p;
+    const float f = m - 1.0f;
+    float p = __fmaf_rn(f, -0.0810155869f, 0.127123073f);
+    p = __fmaf_rn(f, p, -0.129722387f);
+    p = __fmaf_rn(f, p, 0.142021745f);
+    p = __fmaf_rn(f, p, -0.166422471f);
+    p = __fmaf_rn(f, p, 0.200014681f);
+    p = __fmaf_rn(f, p, -0.25000298f);
+    p = __fmaf_rn(f, p, 0.333333284f);
+    const float f2 = f * f;
+    const float lnm = __fmaf_rn(f2, __fmaf_rn(f, p, -0.5f), f);
     const float fe = (float)e;
     // ln2 split so that fe * LN2_HI is exact for |e| < 2^8
     const float ln = __fmaf_rn(fe, 0.693145752f, __fmaf_rn(fe, 1.42860677e-06f, lnm));
@@ -88,14 +92,11 @@ __device__ __forceinline__ void ismc_sincos_2pi(float u, float* s, float* c) {
     cp = __fmaf_rn(r2, cp, 2.53669507e-01f);                       // +(pi/2)^4/4!
     cp = __fmaf_rn(r2, cp, -1.23370055f);                          // -(pi/2)^2/2!
     const float cs = __fmaf_rn(r2, cp, 1.0f);
-    float so, co;
-    switch (q) {
-        case 0: so = sn;  co = cs;  break;
-        case 1: so = cs;  co = -sn; break;
-        case 2: so = -sn; co = -cs; break;
-        default: so = -cs; co = sn; break;
-    }
-    *s = so; *c = co;
+    // quadrant q: (sin, cos) = (sn, cs), (cs, -sn), (-sn, -cs), (-cs, sn), as selects
+    const bool swap = (q & 1) != 0;
+    const float so = swap ? cs : sn, co = swap ? sn : cs;
+    *s = (q & 2) ? -so : so;
+    *c = ((q + 1) & 2) ? -co : co;
 }
 
 // e^-x for x >= 0 (Cody-Waite reduction x = k ln2 + r, |r| <= ln2/2, then the

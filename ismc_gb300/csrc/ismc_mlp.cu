@@ -1,0 +1,665 @@
+// ismc_mlp.cu -- the surrogate network on the 5th-generation tensor cores.
+//
+// MLP 5 -> 256 -> 256 -> 256 -> 6 with SiLU hidden activations, BF16 weights
+// and activations, FP32 accumulation, trained with Adam on a heteroscedastic
+// Gaussian negative log-likelihood.  It maps (ln mu_a, ln mu_s', g, d, n) of a
+// slab between slides to the means of (R_d, T_d, T_u) and their log-variances.
+//
+// Every matrix product is one kernel, umma_gemm_kernel: D = A * B^T with A
+// (M x K) and B (N x K) both K-major BF16 in global memory, tiles brought into
+// shared memory by TMA (128-byte swizzle), multiplied by tcgen05.mma issued
+// from one thread into a TMEM accumulator (128 lanes x BN fp32 columns), and
+// read back by four warps with tcgen05.ld for a fused epilogue:
+//   EPI_HIDDEN  z = acc + b;  H = silu(z) (row- and column-major bf16), G = silu'(z)
+//   EPI_BWD     dz = acc * G  (row- and column-major bf16)
+//   EPI_OUT     z = acc + b   (fp32)
+//   EPI_ACC     atomicAdd(acc) into fp32 (split-K weight gradients)
+// Layer inputs are padded to K = 64 and the output layer to 16 rows, so every
+// product uses the same 64-wide K chunks.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <cmath>
+#include <vector>
+
+#include "ismc_dev.h"
+#include "ismc_umma.cuh"
+
+namespace {
+
+constexpr int BM = 128;           // rows per tile (tcgen05 M)
+constexpr int BK = 64;            // K per stage: 64 bf16 = one 128-byte swizzle row
+constexpr uint32_t WAIT_LIMIT = 1u << 22;   // polls of a bounded try_wait: seconds at most
+
+enum { EPI_HIDDEN = 0, EPI_BWD = 1, EPI_OUT = 2, EPI_ACC = 3 };
+
+struct Epi {
+    int mode;
+    int M, N;                      // valid rows / columns of D
+    const float* bias;             // [N]
+    const __nv_bfloat16* gate;     // [M x ldg] (EPI_BWD)
+    int ldg;
+    __nv_bfloat16* out_row;        // [M x ldr]
+    int ldr;
+    __nv_bfloat16* out_col;        // [N x ldc] (transposed copy)
+    int ldc;
+    __nv_bfloat16* out_aux;        // [M x lda]  silu'(z)
+    int lda;
+    float* out_f;                  // [M x ldf]
+    int ldf;
+};
+
+__device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + __expf(-z)); }
+
+template <int BN>
+__global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ CUtensorMap tA,
+                                                        const __grid_constant__ CUtensorMap tB,
+                                                        int k_chunks, Epi e, int* err) {
+    static_assert(BN >= 16 && BN <= 256 && BN % 16 == 0, "tile N");
+    constexpr uint32_t A_BYTES = BM * BK * 2;
+    constexpr uint32_t B_BYTES = BN * BK * 2;
+    constexpr uint32_t STAGE = A_BYTES + B_BYTES;
+    constexpr uint32_t TCOLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+    constexpr uint32_t IDESC = umma::idesc_bf16_f32(BM, BN);
+
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * STAGE);   // full[2], done[2], fin
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 5);
+    int* sfail = reinterpret_cast<int*>(tslot + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    const int kc0 = blockIdx.z * k_chunks;                 // split-K slice
+
+    if (warp == 0) {
+        umma::tmem_alloc(umma::smem_u32(tslot), TCOLS);
+        umma::tmem_relinquish();
+    }
+    if (threadIdx.x == 32) {
+        for (int i = 0; i < 5; ++i) umma::mbar_init(umma::smem_u32(bars + i), 1);
+        *sfail = 0;
+        umma::fence_barrier_init();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tslot;
+
+    if (threadIdx.x == 0) {
+        const uint32_t sa0 = umma::smem_u32(smem), sb0 = sa0 + A_BYTES;
+        auto load = [&](int kc, int s) {
+            const uint32_t bar = umma::smem_u32(bars + s);
+            umma::mbar_expect_tx(bar, STAGE);
+            umma::tma_load_2d(sa0 + s * STAGE, &tA, (kc0 + kc) * BK, m0, bar);
+            umma::tma_load_2d(sb0 + s * STAGE, &tB, (kc0 + kc) * BK, n0, bar);
+        };
+        bool ok = true;
+        load(0, 0);
+        for (int kc = 0; kc < k_chunks && ok; ++kc) {
+            const int s = kc & 1;
+            if (kc + 1 < k_chunks) {
+                const int s1 = (kc + 1) & 1;
+                // stage s1 was read by the MMAs of chunk kc-1
+                if (kc >= 1 && !umma::mbar_wait(umma::smem_u32(bars + 2 + s1), ((kc - 1) >> 1) & 1,
+                                                 WAIT_LIMIT)) { ok = false; break; }
+                load(kc + 1, s1);
+            }
+            if (!umma::mbar_wait(umma::smem_u32(bars + s), (kc >> 1) & 1, WAIT_LIMIT)) {
+                ok = false;
+                break;
+            }
+            umma::fence_after_sync();
+            const uint64_t da = umma::desc_sw128(sa0 + s * STAGE);
+            const uint64_t db = umma::desc_sw128(sb0 + s * STAGE);
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk)     // 16 bf16 = 32 B per MMA: +2 in the address field
+                umma::mma_bf16(tmem, da + 2 * kk, db + 2 * kk, IDESC, (kc | kk) != 0);
+            umma::mma_commit(umma::smem_u32(bars + 2 + s));
+        }
+        if (ok) umma::mma_commit(umma::smem_u32(bars + 4));
+        else *sfail = 1;
+    }
+    __syncthreads();
+    bool ok = *sfail == 0;
+    if (ok) ok = umma::mbar_wait(umma::smem_u32(bars + 4), 0, WAIT_LIMIT);
+    if (!ok) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+    } else {
+        umma::fence_after_sync();
+        const int r = m0 + warp * 32 + lane;                 // this thread's row
+        const bool row_ok = r < e.M;
+#pragma unroll 1
+        for (int c = 0; c < BN; c += 16) {
+            float v[16];
+            umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+            const int nb = n0 + c;
+            if (!row_ok) continue;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int n = nb + j;
+                if (n >= e.N) break;
+                float x = v[j];
+                switch (e.mode) {
+                    case EPI_HIDDEN: {
+                        const float z = x + e.bias[n];
+                        const float sg = sigmoidf_(z);
+                        const float h = z * sg;
+                        const __nv_bfloat16 hb = __float2bfloat16_rn(h);
+                        e.out_row[(size_t)r * e.ldr + n] = hb;
+                        e.out_col[(size_t)n * e.ldc + r] = hb;
+                        e.out_aux[(size_t)r * e.lda + n] =
+                            __float2bfloat16_rn(sg * (1.0f + z * (1.0f - sg)));
+                        break;
+                    }
+                    case EPI_BWD: {
+                        const float dz = x * __bfloat162float(e.gate[(size_t)r * e.ldg + n]);
+                        const __nv_bfloat16 b = __float2bfloat16_rn(dz);
+                        e.out_row[(size_t)r * e.ldr + n] = b;
+                        e.out_col[(size_t)n * e.ldc + r] = b;
+                        break;
+                    }
+                    case EPI_OUT:
+                        e.out_f[(size_t)r * e.ldf + n] = x + e.bias[n];
+                        break;
+                    default:
+                        atomicAdd(e.out_f + (size_t)r * e.ldf + n, x);
+                        break;
+                }
+            }
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, TCOLS);
+}
+
+template <int BN>
+constexpr size_t gemm_smem() {
+    return 1024 + 2 * (size_t)(BM * BK * 2 + BN * BK * 2) + 5 * 8 + 16;
+}
+
+// --------------------------------------------------------------------------
+// small kernels
+// --------------------------------------------------------------------------
+struct Norm { float lo[5], hi[5]; };
+
+// raw inputs [B x 5] -> bf16 X0 [B x 64] (row) and X0T [64 x B] (column),
+// each feature mapped to [-1, 1]; padding columns are zero.
+__global__ void prep_inputs(const float* __restrict__ x, int B, Norm nm, __nv_bfloat16* X0,
+                            __nv_bfloat16* X0T) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= B) return;
+    for (int k = 0; k < 64; ++k) {
+        float f = 0.0f;
+        if (k < 5) f = 2.0f * (x[(size_t)r * 5 + k] - nm.lo[k]) / (nm.hi[k] - nm.lo[k]) - 1.0f;
+        const __nv_bfloat16 b = __float2bfloat16_rn(f);
+        X0[(size_t)r * 64 + k] = b;
+        X0T[(size_t)k * B + r] = b;
+    }
+}
+
+// Gaussian NLL: out O [B x 16] fp32 (mu in cols 0-2, log-variance in 3-5),
+// targets y [B x 3].  loss = mean_b sum_k 0.5 (exp(-s)(y-mu)^2 + s);
+// dO (bf16 [B x 64] row, [64 x B] column; unused columns zero) = dloss/dO.
+__global__ void nll_loss_grad(const float* __restrict__ O, const float* __restrict__ y, int B,
+                              float inv_b, __nv_bfloat16* dO, __nv_bfloat16* dOT, float* loss) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.0f;
+    if (r < B) {
+        for (int k = 0; k < 64; ++k) {
+            float g = 0.0f;
+            if (k < 3) {
+                const float mu = O[(size_t)r * 16 + k], s = O[(size_t)r * 16 + 3 + k];
+                const float d = y[(size_t)r * 3 + k] - mu;
+                const float ie = __expf(-s);
+                l += 0.5f * (ie * d * d + s);
+                g = -ie * d * inv_b;
+            } else if (k < 6) {
+                const float mu = O[(size_t)r * 16 + k - 3], s = O[(size_t)r * 16 + k];
+                const float d = y[(size_t)r * 3 + k - 3] - mu;
+                g = 0.5f * (1.0f - __expf(-s) * d * d) * inv_b;
+            }
+            const __nv_bfloat16 b = __float2bfloat16_rn(g);
+            dO[(size_t)r * 64 + k] = b;
+            dOT[(size_t)k * B + r] = b;
+        }
+    }
+    // block reduction of the loss
+    __shared__ float red[256];
+    red[threadIdx.x] = l;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(loss, red[0] * inv_b);
+}
+
+// db[n] = sum_b dZT[n][b]  (one block per row n)
+__global__ void bias_grad(const __nv_bfloat16* __restrict__ dZT, int B, int N, float* db) {
+    const int n = blockIdx.x;
+    if (n >= N) return;
+    float s = 0.0f;
+    for (int b = threadIdx.x; b < B; b += blockDim.x) s += __bfloat162float(dZT[(size_t)n * B + b]);
+    __shared__ float red[256];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[n] = red[0];
+}
+
+// One parameter tensor: fp32 master w [R x C], gradient g, Adam moments m, v;
+// writes the bf16 copies used by the GEMMs: W [R x ldw] (row, K-major for the
+// forward) and WT [C x ldt] (transposed, K-major for the backward).
+__global__ void adam_update(float* w, const float* g, float* m, float* v, int R, int C, float lr,
+                            float b1, float b2, float eps, float bc1, float bc2,
+                            __nv_bfloat16* W, int ldw, __nv_bfloat16* WT, int ldt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R * C) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    w[i] = wi;
+    const int r = i / C, c = i % C;
+    const __nv_bfloat16 b = __float2bfloat16_rn(wi);
+    if (W) W[(size_t)r * ldw + c] = b;
+    if (WT) WT[(size_t)c * ldt + r] = b;
+}
+
+// bf16 copies of a parameter tensor without an update
+__global__ void cast_params(const float* w, int R, int C, __nv_bfloat16* W, int ldw,
+                            __nv_bfloat16* WT, int ldt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R * C) return;
+    const int r = i / C, c = i % C;
+    const __nv_bfloat16 b = __float2bfloat16_rn(w[i]);
+    if (W) W[(size_t)r * ldw + c] = b;
+    if (WT) WT[(size_t)c * ldt + r] = b;
+}
+
+}  // namespace
+
+// ==========================================================================
+// host side
+// ==========================================================================
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// layer shapes (out x in), padded storage (rows x K)
+static const int kOut[4] = {256, 256, 256, 6};
+static const int kIn[4] = {5, 256, 256, 256};
+static const int kRowsPad[4] = {256, 256, 256, 16};   // rows of the bf16 W used as B operand
+static const int kKPad[4] = {64, 256, 256, 256};      // K of the forward product
+static const int kWTRows[4] = {64, 256, 256, 256};    // rows of WT (= padded in)
+static const int kWTK[4] = {256, 256, 256, 64};       // K of the backward-data product
+
+struct ismc_mlp {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int max_batch = 0;
+    EncodeTiledFn encode = nullptr;
+    int* d_err = nullptr;
+    float* d_loss = nullptr;
+    // parameters: fp32 master, grads, Adam moments (one flat buffer each)
+    size_t nparam = 0;
+    size_t off_w[4], off_b[4];
+    float *d_w = nullptr, *d_g = nullptr, *d_m = nullptr, *d_v = nullptr;
+    // bf16 operands
+    __nv_bfloat16* Wb[4] = {};   // [kRowsPad x kKPad]
+    __nv_bfloat16* WTb[4] = {};  // [kWTRows x kWTK]
+    // activations
+    __nv_bfloat16 *X0 = nullptr, *X0T = nullptr;
+    __nv_bfloat16 *H[3] = {}, *HT[3] = {}, *G[3] = {};
+    __nv_bfloat16 *dZ[3] = {}, *dZT[3] = {};
+    __nv_bfloat16 *dO = nullptr, *dOT = nullptr;
+    float* O = nullptr;
+    int adam_t = 0;
+    char err[512] = {0};
+};
+
+static int mlp_err(ismc_mlp* m, int code, const char* msg, cudaError_t e = cudaSuccess) {
+    if (m) snprintf(m->err, sizeof m->err, "%s%s%s", msg, e ? ": " : "", e ? cudaGetErrorString(e) : "");
+    return ismc_lib_error(code, "%s%s%s", msg, e ? ": " : "", e ? cudaGetErrorString(e) : "");
+}
+
+#define MCK(call)                                                                     \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess) return mlp_err(m, ISMC_ERR_CUDA, #call, e_);           \
+    } while (0)
+
+static int make_map(ismc_mlp* m, CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols,
+                    uint32_t box_rows) {
+    // bf16 [rows x cols], cols contiguous; box 64 x box_rows, 128-byte swizzle
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * 2};
+    const cuuint32_t box[2] = {64, box_rows};
+    const cuuint32_t es[2] = {1, 1};
+    CUresult r = m->encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims,
+                           strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return mlp_err(m, ISMC_ERR_INTERNAL, "cuTensorMapEncodeTiled failed");
+    return 0;
+}
+
+template <int BN>
+static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, int N,
+                       const Epi& e, int splits = 1) {
+    // A: [M x K] bf16, B: [N x K] bf16, both K-major; M % 128 == 0, N % BN == 0, K % 64 == 0
+    if (M % BM || N % BN || K % (BK * splits))
+        return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: shape not tileable");
+    CUtensorMap ta, tb;
+    int rc = make_map(m, &ta, A, (uint64_t)M, (uint64_t)K, BM);
+    if (rc) return rc;
+    rc = make_map(m, &tb, B, (uint64_t)N, (uint64_t)K, BN);
+    if (rc) return rc;
+    const size_t smem = gemm_smem<BN>();
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(umma_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        attr_set = true;
+    }
+    dim3 grid(M / BM, N / BN, splits);
+    umma_gemm_kernel<BN><<<grid, 128, smem, m->stream>>>(ta, tb, K / BK / splits, e, m->d_err);
+    cudaError_t err = cudaGetLastError();
+    return err == cudaSuccess ? 0 : mlp_err(m, ISMC_ERR_CUDA, "gemm launch", err);
+}
+
+static Norm g_norm = {{-4.605170186f, 0.0f, 0.6f, 0.02f, 1.33f},     // ln 0.01, ln 1
+                      {2.302585093f, 4.605170186f, 0.95f, 0.5f, 1.5f}};  // ln 10, ln 100
+
+extern "C" int ismc_mlp_destroy(ismc_mlp* m) {
+    if (!m) return ISMC_ERR_INVALID_ARG;
+    cudaSetDevice(m->device);
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    cudaFree(m->d_err); cudaFree(m->d_loss);
+    cudaFree(m->d_w); cudaFree(m->d_g); cudaFree(m->d_m); cudaFree(m->d_v);
+    for (int l = 0; l < 4; ++l) { cudaFree(m->Wb[l]); cudaFree(m->WTb[l]); }
+    cudaFree(m->X0); cudaFree(m->X0T);
+    for (int l = 0; l < 3; ++l) {
+        cudaFree(m->H[l]); cudaFree(m->HT[l]); cudaFree(m->G[l]); cudaFree(m->dZ[l]); cudaFree(m->dZT[l]);
+    }
+    cudaFree(m->dO); cudaFree(m->dOT); cudaFree(m->O);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return 0;
+}
+
+static int refresh_bf16(ismc_mlp* m) {
+    for (int l = 0; l < 4; ++l) {
+        const int R = kOut[l], C = kIn[l], n = R * C;
+        cast_params<<<(n + 255) / 256, 256, 0, m->stream>>>(m->d_w + m->off_w[l], R, C, m->Wb[l],
+                                                             kKPad[l], m->WTb[l], kWTK[l]);
+    }
+    MCK(cudaGetLastError());
+    return 0;
+}
+
+extern "C" int ismc_mlp_create(int device, uint32_t max_batch, uint64_t seed, ismc_mlp** out) {
+    if (!out || max_batch == 0 || max_batch % 128)
+        return ismc_lib_error(ISMC_ERR_INVALID_ARG, "mlp_create: max_batch must be a positive multiple of 128");
+    ismc_mlp* m = new ismc_mlp();
+    *out = nullptr;
+    m->device = device;
+    m->max_batch = (int)max_batch;
+    int rc = 0;
+    auto fail = [&](int code) { ismc_mlp_destroy(m); return code; };
+    if (cudaSetDevice(device) != cudaSuccess) return fail(mlp_err(nullptr, ISMC_ERR_NO_DEVICE, "mlp_create: no device"));
+    if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(mlp_err(nullptr, ISMC_ERR_CUDA, "mlp_create: stream"));
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess || !fn)
+        return fail(mlp_err(nullptr, ISMC_ERR_CUDA, "mlp_create: cuTensorMapEncodeTiled unavailable"));
+    m->encode = reinterpret_cast<EncodeTiledFn>(fn);
+    // parameter layout
+    size_t off = 0;
+    for (int l = 0; l < 4; ++l) {
+        m->off_w[l] = off; off += (size_t)kOut[l] * kIn[l];
+        m->off_b[l] = off; off += (size_t)kOut[l];
+    }
+    m->nparam = off;
+    const size_t B = max_batch;
+#define MAL(p, bytes) if (cudaMalloc(&(p), (bytes)) != cudaSuccess) return fail(mlp_err(nullptr, ISMC_ERR_ALLOC, "mlp_create: cudaMalloc"))
+    MAL(m->d_err, sizeof(int));
+    MAL(m->d_loss, sizeof(float));
+    MAL(m->d_w, off * 4); MAL(m->d_g, off * 4); MAL(m->d_m, off * 4); MAL(m->d_v, off * 4);
+    for (int l = 0; l < 4; ++l) {
+        MAL(m->Wb[l], (size_t)kRowsPad[l] * kKPad[l] * 2);
+        MAL(m->WTb[l], (size_t)kWTRows[l] * kWTK[l] * 2);
+    }
+    MAL(m->X0, B * 64 * 2); MAL(m->X0T, B * 64 * 2);
+    for (int l = 0; l < 3; ++l) {
+        MAL(m->H[l], B * 256 * 2); MAL(m->HT[l], B * 256 * 2); MAL(m->G[l], B * 256 * 2);
+        MAL(m->dZ[l], B * 256 * 2); MAL(m->dZT[l], B * 256 * 2);
+    }
+    MAL(m->dO, B * 64 * 2); MAL(m->dOT, 128 * B * 2); MAL(m->O, B * 16 * 4);
+#undef MAL
+    // zero everything that has padding
+    for (int l = 0; l < 4; ++l) {
+        cudaMemsetAsync(m->Wb[l], 0, (size_t)kRowsPad[l] * kKPad[l] * 2, m->stream);
+        cudaMemsetAsync(m->WTb[l], 0, (size_t)kWTRows[l] * kWTK[l] * 2, m->stream);
+    }
+    cudaMemsetAsync(m->dOT, 0, 128 * B * 2, m->stream);
+    cudaMemsetAsync(m->d_m, 0, off * 4, m->stream);
+    cudaMemsetAsync(m->d_v, 0, off * 4, m->stream);
+    cudaMemsetAsync(m->d_err, 0, sizeof(int), m->stream);
+    // He-style initialisation on the host (uniform, variance 2/fan_in), biases 0
+    std::vector<float> w(off, 0.0f);
+    uint64_t s = seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+    auto u = [&]() {
+        s ^= s >> 12; s ^= s << 25; s ^= s >> 27;
+        return (double)((s * 0x2545F4914F6CDD1Dull) >> 11) * (1.0 / 9007199254740992.0);
+    };
+    for (int l = 0; l < 4; ++l) {
+        const double a = std::sqrt(6.0 / kIn[l]) * (l == 3 ? 0.1 : 1.0);
+        for (size_t i = 0; i < (size_t)kOut[l] * kIn[l]; ++i) w[m->off_w[l] + i] = (float)((2 * u() - 1) * a);
+    }
+    if (cudaMemcpyAsync(m->d_w, w.data(), off * 4, cudaMemcpyHostToDevice, m->stream) != cudaSuccess)
+        return fail(mlp_err(nullptr, ISMC_ERR_CUDA, "mlp_create: upload"));
+    rc = refresh_bf16(m);
+    if (rc) return fail(rc);
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess)
+        return fail(mlp_err(nullptr, ISMC_ERR_CUDA, "mlp_create: sync"));
+    *out = m;
+    return 0;
+}
+
+extern "C" size_t ismc_mlp_nparam(void) {
+    size_t n = 0;
+    for (int l = 0; l < 4; ++l) n += (size_t)kOut[l] * kIn[l] + kOut[l];
+    return n;
+}
+
+extern "C" int ismc_mlp_get_params(ismc_mlp* m, float* host, size_t n) {
+    if (!m || !host || n != m->nparam) return ISMC_ERR_INVALID_ARG;
+    MCK(cudaMemcpyAsync(host, m->d_w, n * 4, cudaMemcpyDeviceToHost, m->stream));
+    MCK(cudaStreamSynchronize(m->stream));
+    return 0;
+}
+
+extern "C" int ismc_mlp_set_params(ismc_mlp* m, const float* host, size_t n) {
+    if (!m || !host || n != m->nparam) return ISMC_ERR_INVALID_ARG;
+    MCK(cudaMemcpyAsync(m->d_w, host, n * 4, cudaMemcpyHostToDevice, m->stream));
+    int rc = refresh_bf16(m);
+    if (rc) return rc;
+    MCK(cudaStreamSynchronize(m->stream));
+    m->adam_t = 0;
+    MCK(cudaMemsetAsync(m->d_m, 0, n * 4, m->stream));
+    MCK(cudaMemsetAsync(m->d_v, 0, n * 4, m->stream));
+    return 0;
+}
+
+// forward pass of B rows of raw inputs; leaves H, G and O in the workspace
+static int forward(ismc_mlp* m, const float* d_x, int B) {
+    prep_inputs<<<(B + 127) / 128, 128, 0, m->stream>>>(d_x, B, g_norm, m->X0, m->X0T);
+    MCK(cudaGetLastError());
+    const __nv_bfloat16* in = m->X0;
+    int K = 64;
+    for (int l = 0; l < 3; ++l) {
+        Epi e{};
+        e.mode = EPI_HIDDEN; e.M = B; e.N = 256;
+        e.bias = m->d_w + m->off_b[l];
+        e.out_row = m->H[l]; e.ldr = 256;
+        e.out_col = m->HT[l]; e.ldc = B;
+        e.out_aux = m->G[l]; e.lda = 256;
+        int rc = launch_gemm<256>(m, in, B, K, m->Wb[l], 256, e);
+        if (rc) return rc;
+        in = m->H[l];
+        K = 256;
+    }
+    Epi e{};
+    e.mode = EPI_OUT; e.M = B; e.N = 6;
+    e.bias = m->d_w + m->off_b[3];
+    e.out_f = m->O; e.ldf = 16;
+    return launch_gemm<16>(m, in, B, 256, m->Wb[3], 16, e);
+}
+
+// gradients of the mean loss into m->d_g (and the loss into m->d_loss)
+static int backward(ismc_mlp* m, const float* d_y, int B) {
+    MCK(cudaMemsetAsync(m->d_loss, 0, sizeof(float), m->stream));
+    MCK(cudaMemsetAsync(m->d_g, 0, m->nparam * 4, m->stream));
+    nll_loss_grad<<<(B + 255) / 256, 256, 0, m->stream>>>(m->O, d_y, B, 1.0f / B, m->dO, m->dOT,
+                                                          m->d_loss);
+    MCK(cudaGetLastError());
+    const int splits = B >= 2048 ? 16 : (B >= 512 ? 4 : 1);
+    // output layer: dW4 [6 x 256] = dO^T H3, db4, dZ3 = (dO W4) * G3
+    {
+        Epi e{};
+        e.mode = EPI_ACC; e.M = 6; e.N = 256; e.out_f = m->d_g + m->off_w[3]; e.ldf = 256;
+        int rc = launch_gemm<256>(m, m->dOT, 128, B, m->HT[2], 256, e, splits);
+        if (rc) return rc;
+        bias_grad<<<6, 256, 0, m->stream>>>(m->dOT, B, 6, m->d_g + m->off_b[3]);
+        Epi d{};
+        d.mode = EPI_BWD; d.M = B; d.N = 256; d.gate = m->G[2]; d.ldg = 256;
+        d.out_row = m->dZ[2]; d.ldr = 256; d.out_col = m->dZT[2]; d.ldc = B;
+        rc = launch_gemm<256>(m, m->dO, B, 64, m->WTb[3], 256, d);
+        if (rc) return rc;
+    }
+    for (int l = 2; l >= 0; --l) {
+        // dW_l [256 x in] = dZ_l^T X_{l}, db_l
+        const __nv_bfloat16* XT = l ? m->HT[l - 1] : m->X0T;
+        const int Kin = l ? 256 : 64;
+        Epi e{};
+        e.mode = EPI_ACC; e.M = 256; e.N = kIn[l]; e.out_f = m->d_g + m->off_w[l]; e.ldf = kIn[l];
+        int rc = Kin == 256 ? launch_gemm<256>(m, m->dZT[l], 256, B, XT, 256, e, splits)
+                            : launch_gemm<64>(m, m->dZT[l], 256, B, XT, 64, e, splits);
+        if (rc) return rc;
+        bias_grad<<<256, 256, 0, m->stream>>>(m->dZT[l], B, 256, m->d_g + m->off_b[l]);
+        if (l == 0) break;
+        // dZ_{l-1} = (dZ_l W_l) * G_{l-1}
+        Epi d{};
+        d.mode = EPI_BWD; d.M = B; d.N = 256; d.gate = m->G[l - 1]; d.ldg = 256;
+        d.out_row = m->dZ[l - 1]; d.ldr = 256; d.out_col = m->dZT[l - 1]; d.ldc = B;
+        rc = launch_gemm<256>(m, m->dZ[l], B, 256, m->WTb[l], 256, d);
+        if (rc) return rc;
+    }
+    MCK(cudaGetLastError());
+    return 0;
+}
+
+static int check_err(ismc_mlp* m) {
+    int h = 0;
+    MCK(cudaMemcpyAsync(&h, m->d_err, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+    MCK(cudaStreamSynchronize(m->stream));
+    if (h) return mlp_err(m, ISMC_ERR_INTERNAL, "tensor-core pipeline wait timed out");
+    return 0;
+}
+
+extern "C" int ismc_mlp_forward(ismc_mlp* m, const float* d_x, uint32_t B, float* d_out) {
+    if (!m || !d_x || !d_out || B == 0 || B % 128 || (int)B > m->max_batch)
+        return ISMC_ERR_INVALID_ARG;
+    MCK(cudaSetDevice(m->device));
+    int rc = forward(m, d_x, (int)B);
+    if (rc) return rc;
+    MCK(cudaMemcpy2DAsync(d_out, 6 * 4, m->O, 16 * 4, 6 * 4, B, cudaMemcpyDeviceToDevice, m->stream));
+    return check_err(m);
+}
+
+extern "C" int ismc_mlp_grad(ismc_mlp* m, const float* d_x, const float* d_y, uint32_t B,
+                             float* d_grad, float* loss) {
+    if (!m || !d_x || !d_y || B == 0 || B % 128 || (int)B > m->max_batch)
+        return ISMC_ERR_INVALID_ARG;
+    MCK(cudaSetDevice(m->device));
+    int rc = forward(m, d_x, (int)B);
+    if (rc) return rc;
+    rc = backward(m, d_y, (int)B);
+    if (rc) return rc;
+    if (d_grad) MCK(cudaMemcpyAsync(d_grad, m->d_g, m->nparam * 4, cudaMemcpyDeviceToDevice, m->stream));
+    if (loss) MCK(cudaMemcpyAsync(loss, m->d_loss, 4, cudaMemcpyDeviceToHost, m->stream));
+    return check_err(m);
+}
+
+extern "C" int ismc_mlp_train_step(ismc_mlp* m, const float* d_x, const float* d_y, uint32_t B,
+                                   float lr, float* loss) {
+    if (!m || !d_x || !d_y || B == 0 || B % 128 || (int)B > m->max_batch)
+        return ISMC_ERR_INVALID_ARG;
+    MCK(cudaSetDevice(m->device));
+    int rc = forward(m, d_x, (int)B);
+    if (rc) return rc;
+    rc = backward(m, d_y, (int)B);
+    if (rc) return rc;
+    ++m->adam_t;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float bc1 = 1.0f - powf(b1, (float)m->adam_t), bc2 = 1.0f - powf(b2, (float)m->adam_t);
+    for (int l = 0; l < 4; ++l) {
+        const int R = kOut[l], C = kIn[l];
+        adam_update<<<(R * C + 255) / 256, 256, 0, m->stream>>>(
+            m->d_w + m->off_w[l], m->d_g + m->off_w[l], m->d_m + m->off_w[l], m->d_v + m->off_w[l],
+            R, C, lr, b1, b2, eps, bc1, bc2, m->Wb[l], kKPad[l], m->WTb[l], kWTK[l]);
+        adam_update<<<(R + 255) / 256, 256, 0, m->stream>>>(
+            m->d_w + m->off_b[l], m->d_g + m->off_b[l], m->d_m + m->off_b[l], m->d_v + m->off_b[l],
+            R, 1, lr, b1, b2, eps, bc1, bc2, nullptr, 0, nullptr, 0);
+    }
+    MCK(cudaGetLastError());
+    if (loss) {
+        MCK(cudaMemcpyAsync(loss, m->d_loss, 4, cudaMemcpyDeviceToHost, m->stream));
+        return check_err(m);
+    }
+    return 0;
+}
+
+extern "C" int ismc_mlp_sync(ismc_mlp* m) {
+    if (!m) return ISMC_ERR_INVALID_ARG;
+    return check_err(m);
+}
+
+// Plain GEMM through the same kernel, for tests: D[M x N] fp32 = A[M x K] B[N x K]^T
+// with bf16 device operands (M % 128 == 0, N % 256 == 0 or N == 16 or 64, K % 64 == 0).
+extern "C" int ismc_mlp_gemm_test(ismc_mlp* m, const void* A, const void* Bm, float* D, int M, int N,
+                                  int K, int splits) {
+    if (!m || !A || !Bm || !D) return ISMC_ERR_INVALID_ARG;
+    MCK(cudaSetDevice(m->device));
+    MCK(cudaMemsetAsync(D, 0, (size_t)M * N * 4, m->stream));
+    Epi e{};
+    e.mode = EPI_ACC; e.M = M; e.N = N; e.out_f = D; e.ldf = N;
+    int rc;
+    if (N % 256 == 0) rc = launch_gemm<256>(m, A, M, K, Bm, N, e, splits);
+    else if (N % 64 == 0) rc = launch_gemm<64>(m, A, M, K, Bm, N, e, splits);
+    else rc = launch_gemm<16>(m, A, M, K, Bm, N, e, splits);
+    if (rc) return rc;
+    return check_err(m);
+}
+
+extern "C" int ismc_mlp_last_error(const ismc_mlp* m, char* buf, size_t n) {
+    if (!m || !buf || !n) return ISMC_ERR_INVALID_ARG;
+    snprintf(buf, n, "%s", m->err);
+    return 0;
+}

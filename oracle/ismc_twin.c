@@ -49,13 +49,17 @@ static float neglog_u32(uint32_t x) {
     int e = (int)(b >> 23) - 127;
     float m = f_of((b & 0x007FFFFFu) | 0x3F800000u);
     if (m > 1.41421354f) { m = m * 0.5f; e += 1; }
-    const float t = (m - 1.0f) / (m + 1.0f);
-    const float t2 = t * t;
-    float p = fmaf(t2, 0.111111112f, 0.142857149f);
-    p = fmaf(t2, p, 0.200000003f);
-    p = fmaf(t2, p, 0.333333343f);
-    p = fmaf(t2, p, 1.0f);
-    const float lnm = (2.0f * t) * p;
+    /* ln m = f - f^2/2 + f^3 Q(f), f = m - 1, Q degree 7 (least squares) */
+    const float f = m - 1.0f;
+    float p = fmaf(f, -0.0810155869f, 0.127123073f);
+    p = fmaf(f, p, -0.129722387f);
+    p = fmaf(f, p, 0.142021745f);
+    p = fmaf(f, p, -0.166422471f);
+    p = fmaf(f, p, 0.200014681f);
+    p = fmaf(f, p, -0.25000298f);
+    p = fmaf(f, p, 0.333333284f);
+    const float f2 = f * f;
+    const float lnm = fmaf(f2, fmaf(f, p, -0.5f), f);
     const float fe = (float)e;
     const float ln = fmaf(fe, 0.693145752f, fmaf(fe, 1.42860677e-06f, lnm));
     return -ln;
@@ -197,11 +201,10 @@ typedef struct {
 
 static void run_packet(const TwinInst* I, uint64_t id, uint32_t max_events, TwinPacket* o) {
     const int compat = I->mode == ISMC_MODE_COMPAT;
-    const float INF = f_of(0x7f800000u);
     uint32_t ev = 0, steps = 0, reinc = 0;
     int incident = 1, side = 0, layer = 0;
     float w = 1.0f, absorbed = 0.0f, z = 0.0f, tau = 0.0f;
-    float ux = I->ux0, uy = 0.0f, uz = I->uz0, inv_uz = 1.0f;
+    float ux = I->ux0, uy = 0.0f, uz = I->uz0;
     int bin = -1, fin = 0;
     while (!fin) {
         uint32_t r[4] = {ev, (uint32_t)id, (uint32_t)(id >> 32), I->stream};
@@ -233,7 +236,6 @@ static void run_packet(const TwinInst* I, uint64_t id, uint32_t max_events, Twin
                 ux = ux * eta;
                 uy = uy * eta;
                 uz = top ? ct : -ct;
-                inv_uz = 1.0f / uz;
                 z = top ? 0.0f : I->t_tot;
                 layer = l;
                 incident = 0;
@@ -246,14 +248,18 @@ static void run_packet(const TwinInst* I, uint64_t id, uint32_t max_events, Twin
             const int down = uz > 0.0f;
             const int glass = I->glass[l];
             const float zb = down ? I->z_bot[l] : I->z_top[l];
-            const float d = (uz == 0.0f) ? INF : fmaxf((zb - z) * inv_uz, 0.0f);
+            const float dist = fmaxf(down ? zb - z : z - zb, 0.0f);
+            const float auz = fabsf(uz);
             const float mut = I->mut[l];
-            if (glass && uz == 0.0f) {
+            if (glass && auz == 0.0f) {
                 fin = 2;
-            } else if (glass || tau >= d * mut) {
+            } else if (glass || (auz > 0.0f && dist * mut <= tau * auz)) {
+                /* the free path tau/mut reaches the boundary at dist/|uz| */
                 if (!glass) {
+                    const float d = dist / auz;
                     tau = fmaxf(fmaf(-d, mut, tau), 0.0f);
                 } else if (!compat && I->drop[l] > 0.0f) {
+                    const float d = dist / auz;
                     const float wn = w * expneg(I->drop[l] * d);
                     absorbed = absorbed + (w - wn);
                     w = wn;
@@ -262,10 +268,9 @@ static void run_packet(const TwinInst* I, uint64_t id, uint32_t max_events, Twin
                 const int nl = down ? l + 1 : l - 1;
                 const float eta = down ? I->eta_dn[l] : I->eta_up[l];
                 float ct;
-                const float R = fresnel(eta, fabsf(uz), &ct);
+                const float R = fresnel(eta, auz, &ct);
                 if (u0 < R) {
                     uz = -uz;
-                    inv_uz = -inv_uz;
                 } else if (nl < 0 || nl >= (int)I->L) {
                     side = nl < 0 ? 0 : 1;
                     to_sphere = 1;
@@ -274,7 +279,6 @@ static void run_packet(const TwinInst* I, uint64_t id, uint32_t max_events, Twin
                     ux = ux * eta;
                     uy = uy * eta;
                     uz = down ? ct : -ct;
-                    inv_uz = 1.0f / uz;
                     if (compat && glass && !I->glass[nl]) tau = 0.0f;
                     layer = nl;
                     if (I->glass[nl] && trapped_in(I, nl, uz)) fin = 3;
@@ -302,23 +306,24 @@ static void run_packet(const TwinInst* I, uint64_t id, uint32_t max_events, Twin
                     }
                     float sp, cp;
                     sincos_2pi(u2, &sp, &cp);
-                    const float sth = sqrtf(fmaxf(fmaf(-cth, cth, 1.0f), 0.0f));
+                    const float s2 = fmaxf(fmaf(-cth, cth, 1.0f), 0.0f);
                     if (fabsf(uz) > 0.99999f) {
+                        const float sth = sqrtf(s2);
                         ux = sth * cp;
                         uy = sth * sp;
                         uz = uz > 0.0f ? cth : -cth;
                     } else {
-                        /* sqrt(ux^2 + uy^2) = sqrt(1 - uz^2) for a unit vector */
-                        const float zs = sqrtf(fmaf(ux, ux, uy * uy));
-                        const float k = sth / zs;
+                        /* rho2 = ux^2 + uy^2 (= 1 - uz^2 for a unit vector),
+                         * k = sin(theta) / sqrt(rho2) */
+                        const float rho2 = fmaf(ux, ux, uy * uy);
+                        const float k = sqrtf(s2 / rho2);
                         const float bx = fmaf(ux * uz, cp, -(uy * sp));
                         const float by = fmaf(uy * uz, cp, ux * sp);
                         const float nx = fmaf(k, bx, ux * cth);
                         const float ny = fmaf(k, by, uy * cth);
-                        const float nz = fmaf(-(sth * cp), zs, uz * cth);
+                        const float nz = fmaf(-(k * cp), rho2, uz * cth);
                         ux = nx; uy = ny; uz = nz;
                     }
-                    inv_uz = 1.0f / uz;
                     tau = neglog_u32(r[3]);
                 }
             }

@@ -1,0 +1,91 @@
+"""Tensor-core (tcgen05) path of the surrogate: the GEMM kernel against an
+FP64 product of the same BF16 operands, the MLP gradients against the FP64
+numpy oracle (oracle/mlp64.py, with BF16 rounding at the same storage points),
+and that training on the GPU lowers the loss."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GEMM_RTOL = 2e-3      # fp32 accumulation of exact bf16 products
+GRAD_RTOL = 3e-2      # relative L2 error of the whole gradient vector
+
+
+@pytest.fixture(scope="module")
+def sur():
+    from ismc_gb300 import build
+    from ismc_gb300.surrogate import Surrogate
+    build.build()
+    s = Surrogate(0, max_batch=4096, seed=3)
+    yield s
+    s.close()
+
+
+@pytest.mark.parametrize("M,N,K,splits", [(128, 256, 64, 1), (256, 256, 256, 1), (512, 16, 256, 1),
+                                          (256, 64, 4096, 16), (128, 256, 4096, 16),
+                                          (4096, 256, 256, 1)])
+def test_umma_gemm_matches_fp64(sur, M, N, K, splits):
+    import torch
+    g = torch.Generator().manual_seed(M * 7 + N + K)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16)
+    B = torch.randn(N, K, generator=g).to(torch.bfloat16)
+    dA, dB = A.cuda(), B.cuda()
+    D = torch.empty(M, N, device="cuda", dtype=torch.float32)
+    rc = sur.lib.ismc_mlp_gemm_test(sur.h, dA.data_ptr(), dB.data_ptr(), D.data_ptr(), M, N, K, splits)
+    assert rc == 0, sur._err(sur.h)
+    ref = A.double() @ B.double().T
+    err = (D.cpu().double() - ref).abs().max().item()
+    scale = ref.abs().max().item()
+    assert err <= GEMM_RTOL * scale, (err, scale)
+
+
+def test_mlp_gradients_vs_fp64_oracle(sur):
+    from oracle import mlp64
+    rng = np.random.default_rng(0)
+    B = 512
+    x = mlp64.LO + (mlp64.HI - mlp64.LO) * rng.random((B, 5))
+    y = rng.random((B, 3)) * [0.5, 0.3, 0.2]
+    p = sur.get_params().astype(np.float64)
+    loss, g = sur.grad(x.astype(np.float32), y.astype(np.float32))
+    # the oracle sees the same fp32 inputs
+    x32, y32 = x.astype(np.float32).astype(np.float64), y.astype(np.float32).astype(np.float64)
+    loss64, g64 = mlp64.loss_and_grad(p, x32, y32, bf16_emulation=True)
+    assert abs(loss - loss64) <= 1e-3 * abs(loss64) + 1e-4, (loss, loss64)
+    rel = np.linalg.norm(g - g64) / np.linalg.norm(g64)
+    assert rel < GRAD_RTOL, rel
+    # and against the exact FP64 network (no bf16): agreement at bf16 resolution
+    _, g_exact = mlp64.loss_and_grad(p, x32, y32, bf16_emulation=False)
+    assert np.dot(g, g_exact) / (np.linalg.norm(g) * np.linalg.norm(g_exact)) > 0.99
+
+
+def test_mlp_forward_matches_oracle(sur):
+    from oracle import mlp64
+    rng = np.random.default_rng(1)
+    x = mlp64.LO + (mlp64.HI - mlp64.LO) * rng.random((300, 5))      # pads to 384 internally
+    out = sur.forward(x.astype(np.float32)).cpu().numpy()
+    ref, _, _ = mlp64.forward(sur.get_params().astype(np.float64),
+                              x.astype(np.float32).astype(np.float64), mlp64.bf16)
+    assert np.max(np.abs(out - ref[:, :6])) < 2e-2 * max(1.0, np.max(np.abs(ref)))
+
+
+def test_mlp_training_lowers_loss():
+    """Fit a smooth synthetic map (stand-in targets; the Monte Carlo data path is
+    exercised by the surrogate-solve test): the loss must fall well below its start."""
+    import torch
+    from ismc_gb300.surrogate import LO, HI, Surrogate
+    s = Surrogate(0, max_batch=4096, seed=11)
+    try:
+        rng = np.random.default_rng(5)
+        X = LO + (HI - LO) * rng.random((32768, 5))
+        u = (X - LO) / (HI - LO)
+        Y = np.stack([0.5 * np.exp(-2 * u[:, 0]) * (0.3 + u[:, 1]), 0.3 * u[:, 3] * (1 - u[:, 0]),
+                      0.2 * np.exp(-3 * u[:, 1] * u[:, 3])], 1)
+        Y = Y + 0.002 * rng.standard_normal(Y.shape)
+        hist = s.train(X.astype(np.float32), Y.astype(np.float32), epochs=12, batch=4096, lr=1e-3)
+        assert hist[-1] < hist[0] - 2.0, hist
+        pred = s.forward(X[:4096].astype(np.float32)).cpu().numpy()[:, :3]
+        assert np.sqrt(np.mean((pred - Y[:4096]) ** 2)) < 0.02
+    finally:
+        s.close()
