@@ -283,6 +283,38 @@ def run_gpu(args, rank, world, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_other_workload(args):
+    """Secondary workloads of the benchmark set (one JSON line each); the
+    default workload above is the headline line."""
+    from ismc_gb300 import Engine, benchmarks, build
+    build.build()
+    eng = Engine(0)
+    s = args.scale
+    if args.workload == "lookup":
+        r = benchmarks.run_lookup(eng, scale=s)
+        line = {"metric": "photons/s", "value": r["photons_per_s"], "unit": "photons/s",
+                "workload": "lookup", "config": {"workload": "64x64 single-slab grid + 512 random "
+                "1-5 layer stacks, budgets log-uniform 1e5-1e7 x scale, one persistent launch",
+                "scale": s}, "result": r}
+    else:
+        sur, r = benchmarks.run_surrogate(
+            eng, n_samples=int((1 << 20) * s) // 4096 * 4096 or 4096,
+            packets=max(1000, int(100_000 * min(1.0, s * 4))), epochs=args.epochs,
+            heldout=32 if s >= 1 else 12,
+            heldout_packets=10_000_000 if s >= 1 else 1_000_000)
+        line = {"workload": "surrogate", "config": {"scale": s, "epochs": args.epochs},
+                "result": r}
+        if args.workload == "solve":
+            sr = benchmarks.run_solve(eng, sur, n_meas=max(256, int(10000 * s)),
+                                      n_plain=max(32, int(200 * min(1.0, 4 * s))))
+            line = {"metric": "inverse solves/s", "value": sr["surrogate_solves_per_s"],
+                    "unit": "solves/s", "workload": "solve",
+                    "config": {"scale": s, "epochs": args.epochs},
+                    "result": sr, "surrogate": r}
+        sur.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -291,9 +323,19 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--packets", type=int, default=PACKETS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["forward", "lookup", "surrogate", "solve"],
+                    default="forward")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="size factor for the secondary workloads (1 = full benchmark size)")
+    ap.add_argument("--epochs", type=int, default=20,
+                    help="training epochs of the surrogate (surrogate and solve workloads)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.workload != "forward":
+        if rank == 0 and args.impl == "gpu":
+            run_other_workload(args)
+        return
     dist = None
     if world > 1:
         import torch.distributed as tdist

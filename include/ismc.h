@@ -281,10 +281,34 @@ int ismc_mlp_grad(ismc_mlp* m, const float* d_x, const float* d_y, uint32_t batc
                   float* d_grad, float* loss /* host, may be NULL */);
 int ismc_mlp_train_step(ismc_mlp* m, const float* d_x, const float* d_y, uint32_t batch,
                         float lr, float* loss /* host; NULL = do not wait */);
+int ismc_mlp_train_epoch(ismc_mlp* m, const float* d_x, const float* d_y, uint32_t n_rows,
+                         uint32_t batch, const float* lrs /* host, n_rows/batch */,
+                         float* loss /* host, last batch, may be NULL */);
 int ismc_mlp_sync(ismc_mlp* m);
 int ismc_mlp_gemm_test(ismc_mlp* m, const void* d_a, const void* d_b, float* d_d, int M, int N,
                        int K, int splits);   /* D = A B^T, bf16 K-major operands, for tests */
 int ismc_mlp_last_error(const ismc_mlp* m, char* buf, size_t n);
+
+/* ------------------------------------------------------------------------
+ * Lookup-table inversion (Lookup/lookup.py:301-489).  Host arrays in and out
+ * (row-major FP64); the table grid is R_i = i h, T_j = j h, h = 100/(N-1), in
+ * percent, indexed [i][j].
+ *   ismc_table_interp: linear interpolation of scattered samples (R, T, value)
+ *     onto the table over the caller's triangulation tri[ntri][3] (Delaunay,
+ *     as scipy.interpolate.griddata builds it, lookup.py:341-345); NaN outside.
+ *   ismc_table_uncertainty: lookup.py:349-376 -- per cell with finite,
+ *     non-negative standard deviations, M normal draws of (R, T), nearest-cell
+ *     values of both tables, 100 * std / value; NaN elsewhere.
+ *   ismc_table_lookup: nearest cell of table_t[T_j][R_i] (the transposed table
+ *     lookup.py returns) for n measurements (lookup.py:467-489).
+ * ------------------------------------------------------------------------ */
+int ismc_table_interp(const double* R, const double* T, const double* val, uint32_t npts,
+                      const int32_t* tri, uint32_t ntri, uint32_t N, double* out);
+int ismc_table_uncertainty(const double* mua, const double* mus, const double* rstd,
+                           const double* tstd, uint32_t N, uint32_t M, uint64_t seed,
+                           double* mua_unc, double* mus_unc);
+int ismc_table_lookup(const double* table_t, uint32_t N, const double* R, const double* T,
+                      uint32_t n, double* out);
 
 /* Sizes of the ABI structs, so bindings can check their own layouts. */
 size_t ismc_sizeof(int which);   /* 0 stack, 1 spheres, 2 instance, 3 tally, 4 tune,

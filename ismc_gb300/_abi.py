@@ -84,7 +84,8 @@ EXPORTS = ("ismc_version", "ismc_init", "ismc_destroy", "ismc_run", "ismc_run_ba
            "ismc_solve_batch", "ismc_praxis", "ismc_run_batch_noalloc",
            "ismc_mlp_create", "ismc_mlp_destroy", "ismc_mlp_nparam", "ismc_mlp_get_params",
            "ismc_mlp_set_params", "ismc_mlp_forward", "ismc_mlp_grad", "ismc_mlp_train_step",
-           "ismc_mlp_sync", "ismc_mlp_gemm_test", "ismc_mlp_last_error")
+           "ismc_mlp_sync", "ismc_mlp_gemm_test", "ismc_mlp_last_error", "ismc_mlp_train_epoch",
+           "ismc_table_interp", "ismc_table_uncertainty", "ismc_table_lookup")
 
 NOALLOC_MAX_INST = 1024
 
@@ -134,12 +135,21 @@ def declare(lib):
     lib.ismc_mlp_grad.argtypes = [V, V, V, C.c_uint32, V, F]
     lib.ismc_mlp_train_step.restype = C.c_int
     lib.ismc_mlp_train_step.argtypes = [V, V, V, C.c_uint32, C.c_float, F]
+    lib.ismc_mlp_train_epoch.restype = C.c_int
+    lib.ismc_mlp_train_epoch.argtypes = [V, V, V, C.c_uint32, C.c_uint32, F, F]
     lib.ismc_mlp_sync.restype = C.c_int
     lib.ismc_mlp_sync.argtypes = [V]
     lib.ismc_mlp_gemm_test.restype = C.c_int
     lib.ismc_mlp_gemm_test.argtypes = [V, V, V, V, C.c_int, C.c_int, C.c_int, C.c_int]
     lib.ismc_mlp_last_error.restype = C.c_int
     lib.ismc_mlp_last_error.argtypes = [V, C.c_char_p, C.c_size_t]
+    D = P(C.c_double)
+    lib.ismc_table_interp.restype = C.c_int
+    lib.ismc_table_interp.argtypes = [D, D, D, C.c_uint32, P(C.c_int32), C.c_uint32, C.c_uint32, D]
+    lib.ismc_table_uncertainty.restype = C.c_int
+    lib.ismc_table_uncertainty.argtypes = [D, D, D, D, C.c_uint32, C.c_uint32, C.c_uint64, D, D]
+    lib.ismc_table_lookup.restype = C.c_int
+    lib.ismc_table_lookup.argtypes = [D, C.c_uint32, D, D, C.c_uint32, D]
     lib.ismc_sizeof.restype = C.c_size_t
     lib.ismc_sizeof.argtypes = [C.c_int]
     for k, cls in SIZEOF_INDEX.items():

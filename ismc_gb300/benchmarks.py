@@ -21,6 +21,9 @@ import numpy as np
 from .api import Engine, make_solve, tally_to_result
 from .workloads import bench_spheres, lookup_grid
 
+# accepted box of the inverse solves: the sampled ranges widened by 2x each way
+SOLVE_LO, SOLVE_HI = (0.005, 0.5), (20.0, 200.0)
+
 
 def run_lookup(engine: Engine, scale=1.0, seed=2, tune=None):
     insts = lookup_grid(seed=seed, scale=scale)
@@ -95,22 +98,27 @@ def run_solve(engine, sur, n_meas=10000, n_plain=200, seed=4, verify_packets=1_0
     k = min(n_plain, n_meas)
     reqs = [make_solve(sample_stack(1.0, 10.0, 0.9, 0.1, 1.4), 1, sph, plain_packets,
                        (meas[i, 0], None, meas[i, 1], meas[i, 2]), x0=(0.3, 10.0), seed=seed + i,
-                       max_evals=400) for i in range(k)]
+                       lo=SOLVE_LO, hi=SOLVE_HI, max_evals=400) for i in range(k)]
     t0 = time.perf_counter()
     outp = engine.solve_batch(reqs)
     t_plain = time.perf_counter() - t0
     xp = np.array([[o.x[0], o.x[1]] for o in outp])
     ev = np.array([o.evals for o in outp])
-    # surrogate path on every measurement
+    # surrogate path on every measurement (after a short warm-up of its kernels)
+    surrogate_solve(sur, engine, meas[:64], sig, verify_packets=1000, fallback=False, seed=seed)
     t1 = time.perf_counter()
     rs = surrogate_solve(sur, engine, meas, sig, verify_packets=verify_packets,
                          plain_packets=plain_packets, seed=seed + 99)
     t_sur = time.perf_counter() - t1
     xs = rs["x"]
+    # the same surrogate path fitting in noise units instead of the plain path's cost
+    rc = surrogate_solve(sur, engine, meas, sig, verify_packets=verify_packets,
+                         plain_packets=plain_packets, seed=seed + 99, objective="chi2")
 
     def rel(x, t):
         e = np.abs(x / t - 1)
-        return {"median": np.median(e, 0).tolist(), "p90": np.percentile(e, 90, 0).tolist()}
+        return {"median": np.median(e, 0).tolist(), "p90": np.percentile(e, 90, 0).tolist(),
+                "within_2pct": np.mean(e <= 0.02, 0).tolist()}
 
     return {"measurements": n_meas, "plain_subsample": k,
             "plain_solves_per_s": k / t_plain, "plain_evals_mean": float(ev.mean()),
@@ -118,5 +126,10 @@ def run_solve(engine, sur, n_meas=10000, n_plain=200, seed=4, verify_packets=1_0
             "surrogate_solves_per_s": n_meas / t_sur,
             "surrogate_rel_err_vs_truth": rel(xs, truth),
             "surrogate_vs_plain_rel_diff": rel(xs[:k], xp),
+            "chi2_objective": {"rel_err_vs_truth": rel(rc["x"], truth),
+                               "vs_plain_rel_diff": rel(rc["x"][:k], xp),
+                               "fallback_rate": float(rc["fallback"].mean()),
+                               "total_s": rc["timing"]["total_s"]},
+            "corrected_rate": float(rs["corrected"].mean()),
             "fallback_rate": float(rs["fallback"].mean()), "surrogate_timing": rs["timing"],
             "speedup": (n_meas / t_sur) / (k / t_plain)}

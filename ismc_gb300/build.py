@@ -1,6 +1,7 @@
 """In-tree build of the native libraries of the package.
 
-    python -m ismc_gb300.build            # builds ismc_gb300/libismc.so
+    python -m ismc_gb300.build            # builds ismc_gb300/libismc.so and the
+                                          # command-line programs in ismc_gb300/bin/
 
 Every CUDA translation unit is compiled for sm_103a only, in parallel, then
 linked into one shared library next to this file.  FMA contraction is off on
@@ -24,10 +25,14 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + os.path.join(ROOT, "include")] + ARCH
 
-SOURCES = ["ismc_kernels.cu", "ismc_capi.cu", "ismc_noalloc.cu", "ismc_mlp.cu",
+SOURCES = ["ismc_kernels.cu", "ismc_capi.cu", "ismc_noalloc.cu", "ismc_mlp.cu", "ismc_table.cu",
            "ismc_praxis.cpp", "ismc_solve.cpp"]
 CXX_FLAGS = ["-O2", "-std=c++20", "-fPIC", "-ffp-contract=off", "-Wall",
              "-I" + os.path.join(ROOT, "include")]
+BIN = os.path.join(HERE, "bin")
+# drop-ins for the reference's compiled programs, under the names its drivers
+# are pointed at (--CUDAsource .../Lookup.o, .../minimize.o)
+PROGRAMS = {"Lookup.o": "cli/cli_lookup.cpp", "minimize.o": "cli/cli_minimize.cpp"}
 
 
 def nvcc():
@@ -75,6 +80,18 @@ def build(verbose_ptxas=False, quiet=True):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.makedirs(BIN, exist_ok=True)
+    for exe, src in PROGRAMS.items():
+        target, srcp = os.path.join(BIN, exe), os.path.join(CSRC, src)
+        if _newer(target, [srcp, os.path.join(CSRC, "cli", "cli_common.h"), LIB, __file__]
+                  + _headers()):
+            continue
+        cmd = [os.environ.get("CXX", "g++"), srcp, "-o", target, "-O2", "-std=c++17", "-Wall",
+               "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(CSRC, "cli"),
+               "-L" + HERE, "-lismc", "-Wl,-rpath,$ORIGIN/..", "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"build of {exe} failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     if logs and not quiet:
         print(logs)
     return LIB

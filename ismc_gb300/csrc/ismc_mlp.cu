@@ -52,6 +52,7 @@ struct Epi {
     int lda;
     float* out_f;                  // [M x ldf]
     int ldf;
+    int fold;                      // EPI_ACC: column n accumulates into n % fold (0: n)
 };
 
 __device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + __expf(-z)); }
@@ -168,7 +169,7 @@ __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ 
                         e.out_f[(size_t)r * e.ldf + n] = x + e.bias[n];
                         break;
                     default:
-                        atomicAdd(e.out_f + (size_t)r * e.ldf + n, x);
+                        atomicAdd(e.out_f + (size_t)r * e.ldf + (e.fold ? n % e.fold : n), x);
                         break;
                 }
             }
@@ -189,41 +190,63 @@ constexpr size_t gemm_smem() {
 // --------------------------------------------------------------------------
 struct Norm { float lo[5], hi[5]; };
 
-// raw inputs [B x 5] -> bf16 X0 [B x 64] (row) and X0T [64 x B] (column),
-// each feature mapped to [-1, 1]; padding columns are zero.
+// raw inputs [B x 5] -> bf16 X0 [B x 64] (row) and X0T [64 x B] (column).
+// Each feature is mapped to f in [-1, 1] and stored as two bf16 columns, the
+// rounded value f_hi = bf16(f) in column k and the remainder bf16(f - f_hi) in
+// column 5 + k; the first layer's weights are stored twice (columns k and
+// 5 + k), so the product sees f to about 16 bits instead of bf16's 8 and the
+// network is smooth in its inputs at the resolution the inverse solver needs.
+// Columns 10-63 are zero.
 __global__ void prep_inputs(const float* __restrict__ x, int B, Norm nm, __nv_bfloat16* X0,
                             __nv_bfloat16* X0T) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= B) return;
+    float f[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+        f[k] = 2.0f * (x[(size_t)r * 5 + k] - nm.lo[k]) / (nm.hi[k] - nm.lo[k]) - 1.0f;
     for (int k = 0; k < 64; ++k) {
-        float f = 0.0f;
-        if (k < 5) f = 2.0f * (x[(size_t)r * 5 + k] - nm.lo[k]) / (nm.hi[k] - nm.lo[k]) - 1.0f;
-        const __nv_bfloat16 b = __float2bfloat16_rn(f);
+        __nv_bfloat16 b = __float2bfloat16_rn(0.0f);
+        if (k < 5) {
+            b = __float2bfloat16_rn(f[k]);
+        } else if (k < 10) {
+            const float hi = __bfloat162float(__float2bfloat16_rn(f[k - 5]));
+            b = __float2bfloat16_rn(f[k - 5] - hi);
+        }
         X0[(size_t)r * 64 + k] = b;
         X0T[(size_t)k * B + r] = b;
     }
 }
 
-// Gaussian NLL: out O [B x 16] fp32 (mu in cols 0-2, log-variance in 3-5),
-// targets y [B x 3].  loss = mean_b sum_k 0.5 (exp(-s)(y-mu)^2 + s);
+// Gaussian NLL with a variance floor: out O [B x 16] fp32 (mu in cols 0-2,
+// log-variance s in 3-5), targets y [B x 3], variance v = exp(s) + floor^2:
+//   loss = mean_b sum_k 0.5 (d^2 / v + ln v),  d = y - mu
+//   dloss/dmu = -d / v,  dloss/ds = 0.5 (e^s / v) (1 - d^2 / v).
+// The floor (the training targets' Monte Carlo noise scale) keeps the
+// per-sample precision weights bounded where the targets are noise-free
+// (e.g. T_u = 0 for thick samples); floor = 0 is the plain Gaussian NLL.
 // dO (bf16 [B x 64] row, [64 x B] column; unused columns zero) = dloss/dO.
 __global__ void nll_loss_grad(const float* __restrict__ O, const float* __restrict__ y, int B,
-                              float inv_b, __nv_bfloat16* dO, __nv_bfloat16* dOT, float* loss) {
+                              float inv_b, float floor2, __nv_bfloat16* dO, __nv_bfloat16* dOT,
+                              float* loss) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     float l = 0.0f;
     if (r < B) {
         for (int k = 0; k < 64; ++k) {
             float g = 0.0f;
-            if (k < 3) {
-                const float mu = O[(size_t)r * 16 + k], s = O[(size_t)r * 16 + 3 + k];
-                const float d = y[(size_t)r * 3 + k] - mu;
-                const float ie = __expf(-s);
-                l += 0.5f * (ie * d * d + s);
-                g = -ie * d * inv_b;
-            } else if (k < 6) {
-                const float mu = O[(size_t)r * 16 + k - 3], s = O[(size_t)r * 16 + k];
-                const float d = y[(size_t)r * 3 + k - 3] - mu;
-                g = 0.5f * (1.0f - __expf(-s) * d * d) * inv_b;
+            if (k < 6) {
+                const int q = k < 3 ? k : k - 3;
+                const float mu = O[(size_t)r * 16 + q], s = O[(size_t)r * 16 + 3 + q];
+                const float d = y[(size_t)r * 3 + q] - mu;
+                const float es = __expf(s);
+                const float v = es + floor2;
+                const float iv = 1.0f / v;
+                if (k < 3) {
+                    l += 0.5f * (d * d * iv + __logf(v));
+                    g = -d * iv * inv_b;
+                } else {
+                    g = 0.5f * es * iv * (1.0f - d * d * iv) * inv_b;
+                }
             }
             const __nv_bfloat16 b = __float2bfloat16_rn(g);
             dO[(size_t)r * 64 + k] = b;
@@ -259,10 +282,11 @@ __global__ void bias_grad(const __nv_bfloat16* __restrict__ dZT, int B, int N, f
 
 // One parameter tensor: fp32 master w [R x C], gradient g, Adam moments m, v;
 // writes the bf16 copies used by the GEMMs: W [R x ldw] (row, K-major for the
-// forward) and WT [C x ldt] (transposed, K-major for the backward).
+// forward; with dup > 0 also at column c + dup, for the first layer's split
+// inputs) and WT [C x ldt] (transposed, K-major for the backward).
 __global__ void adam_update(float* w, const float* g, float* m, float* v, int R, int C, float lr,
                             float b1, float b2, float eps, float bc1, float bc2,
-                            __nv_bfloat16* W, int ldw, __nv_bfloat16* WT, int ldt) {
+                            __nv_bfloat16* W, int ldw, int dup, __nv_bfloat16* WT, int ldt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= R * C) return;
     const float gi = g[i];
@@ -274,18 +298,24 @@ __global__ void adam_update(float* w, const float* g, float* m, float* v, int R,
     w[i] = wi;
     const int r = i / C, c = i % C;
     const __nv_bfloat16 b = __float2bfloat16_rn(wi);
-    if (W) W[(size_t)r * ldw + c] = b;
+    if (W) {
+        W[(size_t)r * ldw + c] = b;
+        if (dup) W[(size_t)r * ldw + c + dup] = b;
+    }
     if (WT) WT[(size_t)c * ldt + r] = b;
 }
 
 // bf16 copies of a parameter tensor without an update
-__global__ void cast_params(const float* w, int R, int C, __nv_bfloat16* W, int ldw,
+__global__ void cast_params(const float* w, int R, int C, __nv_bfloat16* W, int ldw, int dup,
                             __nv_bfloat16* WT, int ldt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= R * C) return;
     const int r = i / C, c = i % C;
     const __nv_bfloat16 b = __float2bfloat16_rn(w[i]);
-    if (W) W[(size_t)r * ldw + c] = b;
+    if (W) {
+        W[(size_t)r * ldw + c] = b;
+        if (dup) W[(size_t)r * ldw + c + dup] = b;
+    }
     if (WT) WT[(size_t)c * ldt + r] = b;
 }
 
@@ -306,6 +336,9 @@ static const int kRowsPad[4] = {256, 256, 256, 16};   // rows of the bf16 W used
 static const int kKPad[4] = {64, 256, 256, 256};      // K of the forward product
 static const int kWTRows[4] = {64, 256, 256, 256};    // rows of WT (= padded in)
 static const int kWTK[4] = {256, 256, 256, 64};       // K of the backward-data product
+// standard-deviation floor of the Gaussian NLL (about the Monte Carlo noise of
+// the 1e5-packet training targets)
+static const float kVarFloor = 3e-4f;
 
 struct ismc_mlp {
     int device = 0;
@@ -328,6 +361,10 @@ struct ismc_mlp {
     __nv_bfloat16 *dO = nullptr, *dOT = nullptr;
     float* O = nullptr;
     int adam_t = 0;
+    // encoded TMA descriptors, keyed by (buffer, shape): the workspace buffers
+    // never move, so each map is encoded once per batch size it is used with
+    struct MapEntry { const void* p; uint64_t rows, cols; uint32_t box; CUtensorMap map; };
+    std::vector<MapEntry> maps;
     char err[512] = {0};
 };
 
@@ -357,6 +394,22 @@ static int make_map(ismc_mlp* m, CUtensorMap* map, const void* base, uint64_t ro
     return 0;
 }
 
+static int get_map(ismc_mlp* m, CUtensorMap* out, const void* base, uint64_t rows,
+                   uint64_t cols, uint32_t box_rows) {
+    for (const auto& e : m->maps)
+        if (e.p == base && e.rows == rows && e.cols == cols && e.box == box_rows) {
+            *out = e.map;
+            return 0;
+        }
+    ismc_mlp::MapEntry e{base, rows, cols, box_rows, {}};
+    int rc = make_map(m, &e.map, base, rows, cols, box_rows);
+    if (rc) return rc;
+    if (m->maps.size() >= 256) m->maps.clear();   // bounded cache
+    m->maps.push_back(e);
+    *out = e.map;
+    return 0;
+}
+
 template <int BN>
 static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, int N,
                        const Epi& e, int splits = 1) {
@@ -364,9 +417,9 @@ static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, 
     if (M % BM || N % BN || K % (BK * splits))
         return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: shape not tileable");
     CUtensorMap ta, tb;
-    int rc = make_map(m, &ta, A, (uint64_t)M, (uint64_t)K, BM);
+    int rc = get_map(m, &ta, A, (uint64_t)M, (uint64_t)K, BM);
     if (rc) return rc;
-    rc = make_map(m, &tb, B, (uint64_t)N, (uint64_t)K, BN);
+    rc = get_map(m, &tb, B, (uint64_t)N, (uint64_t)K, BN);
     if (rc) return rc;
     const size_t smem = gemm_smem<BN>();
     static bool attr_set = false;
@@ -405,7 +458,8 @@ static int refresh_bf16(ismc_mlp* m) {
     for (int l = 0; l < 4; ++l) {
         const int R = kOut[l], C = kIn[l], n = R * C;
         cast_params<<<(n + 255) / 256, 256, 0, m->stream>>>(m->d_w + m->off_w[l], R, C, m->Wb[l],
-                                                             kKPad[l], m->WTb[l], kWTK[l]);
+                                                             kKPad[l], l == 0 ? 5 : 0, m->WTb[l],
+                                                             kWTK[l]);
     }
     MCK(cudaGetLastError());
     return 0;
@@ -421,7 +475,9 @@ extern "C" int ismc_mlp_create(int device, uint32_t max_batch, uint64_t seed, is
     int rc = 0;
     auto fail = [&](int code) { ismc_mlp_destroy(m); return code; };
     if (cudaSetDevice(device) != cudaSuccess) return fail(mlp_err(nullptr, ISMC_ERR_NO_DEVICE, "mlp_create: no device"));
-    if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess)
+    // a blocking stream: its work is ordered after work the caller queued on the
+    // legacy default stream (e.g. the copy or gather that produced d_x / d_y)
+    if (cudaStreamCreateWithFlags(&m->stream, cudaStreamDefault) != cudaSuccess)
         return fail(mlp_err(nullptr, ISMC_ERR_CUDA, "mlp_create: stream"));
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
@@ -536,7 +592,8 @@ static int forward(ismc_mlp* m, const float* d_x, int B) {
 static int backward(ismc_mlp* m, const float* d_y, int B) {
     MCK(cudaMemsetAsync(m->d_loss, 0, sizeof(float), m->stream));
     MCK(cudaMemsetAsync(m->d_g, 0, m->nparam * 4, m->stream));
-    nll_loss_grad<<<(B + 255) / 256, 256, 0, m->stream>>>(m->O, d_y, B, 1.0f / B, m->dO, m->dOT,
+    nll_loss_grad<<<(B + 255) / 256, 256, 0, m->stream>>>(m->O, d_y, B, 1.0f / B,
+                                                          kVarFloor * kVarFloor, m->dO, m->dOT,
                                                           m->d_loss);
     MCK(cudaGetLastError());
     const int splits = B >= 2048 ? 16 : (B >= 512 ? 4 : 1);
@@ -559,6 +616,7 @@ static int backward(ismc_mlp* m, const float* d_y, int B) {
         const int Kin = l ? 256 : 64;
         Epi e{};
         e.mode = EPI_ACC; e.M = 256; e.N = kIn[l]; e.out_f = m->d_g + m->off_w[l]; e.ldf = kIn[l];
+        if (l == 0) { e.N = 10; e.fold = 5; }     // hi and lo input columns share the weights
         int rc = Kin == 256 ? launch_gemm<256>(m, m->dZT[l], 256, B, XT, 256, e, splits)
                             : launch_gemm<64>(m, m->dZT[l], 256, B, XT, 64, e, splits);
         if (rc) return rc;
@@ -623,10 +681,10 @@ extern "C" int ismc_mlp_train_step(ismc_mlp* m, const float* d_x, const float* d
         const int R = kOut[l], C = kIn[l];
         adam_update<<<(R * C + 255) / 256, 256, 0, m->stream>>>(
             m->d_w + m->off_w[l], m->d_g + m->off_w[l], m->d_m + m->off_w[l], m->d_v + m->off_w[l],
-            R, C, lr, b1, b2, eps, bc1, bc2, m->Wb[l], kKPad[l], m->WTb[l], kWTK[l]);
+            R, C, lr, b1, b2, eps, bc1, bc2, m->Wb[l], kKPad[l], l == 0 ? 5 : 0, m->WTb[l], kWTK[l]);
         adam_update<<<(R + 255) / 256, 256, 0, m->stream>>>(
             m->d_w + m->off_b[l], m->d_g + m->off_b[l], m->d_m + m->off_b[l], m->d_v + m->off_b[l],
-            R, 1, lr, b1, b2, eps, bc1, bc2, nullptr, 0, nullptr, 0);
+            R, 1, lr, b1, b2, eps, bc1, bc2, nullptr, 0, 0, nullptr, 0);
     }
     MCK(cudaGetLastError());
     if (loss) {
@@ -634,6 +692,23 @@ extern "C" int ismc_mlp_train_step(ismc_mlp* m, const float* d_x, const float* d
         return check_err(m);
     }
     return 0;
+}
+
+// One pass over n_rows device-resident rows in batches of `batch` (rows
+// beyond the last whole batch are skipped), Adam learning rate lrs[step] from
+// a host array of n_rows / batch entries; *loss receives the last batch's loss.
+extern "C" int ismc_mlp_train_epoch(ismc_mlp* m, const float* d_x, const float* d_y, uint32_t n_rows,
+                                    uint32_t batch, const float* lrs, float* loss) {
+    if (!m || !d_x || !d_y || !lrs || batch == 0 || batch % 128 || (int)batch > m->max_batch)
+        return ISMC_ERR_INVALID_ARG;
+    const uint32_t steps = n_rows / batch;
+    for (uint32_t s = 0; s < steps; ++s) {
+        const bool last = s + 1 == steps;
+        int rc = ismc_mlp_train_step(m, d_x + (size_t)s * batch * 5, d_y + (size_t)s * batch * 3,
+                                     batch, lrs[s], last ? loss : nullptr);
+        if (rc) return rc;
+    }
+    return check_err(m);
 }
 
 extern "C" int ismc_mlp_sync(ismc_mlp* m) {

@@ -59,6 +59,11 @@ int build_request(Solve& s, uint32_t index, const double* p, std::vector<ismc_in
     s.first = (int)out.size();
     s.count = 0;
     if (!(mua > 0) || !(musr > 0) || !std::isfinite(mua) || !std::isfinite(musr)) return 0;
+    // outside the accepted box the objective is infinite without simulating:
+    // the reference rejects such answers afterwards (minimization.py:267), and
+    // simulating there (e.g. mu_s' of 1e4 /cm: ~1e5 steps per packet) would
+    // stall the whole batched round
+    if (mua < r.lo[0] || mua > r.hi[0] || musr < r.lo[1] || musr > r.hi[1]) return 0;
     ismc_instance base = r.base;
     const uint32_t l = r.layer;
     const double g = base.stack.g[l];

@@ -10,9 +10,12 @@ spheres (separate=False) or twice -- R sphere only and T sphere only
 deviation over repeats of R_d and T_d, arrays of shape (len(mu_a), len(mu_s')),
 as lookup.py:254-257 does (np.std, ddof=0).
 """
+import ctypes as C
+
 import numpy as np
 
-from .api import Layer, Spheres, default_engine, make_instance
+from . import _abi
+from .api import IsmcError, Layer, Spheres, default_engine, load_library, make_instance
 
 
 def _slab(n, mua, mus, g, t, slides):
@@ -20,6 +23,42 @@ def _slab(n, mua, mus, g, t, slides):
     if slides is None:
         return [tissue]
     return [slides[0], tissue, slides[1]]
+
+
+def _grid_instances(mu_a, mu_s_reduced, g, t, n, spheres, N, runs, separate, seed, stream0,
+                    slides, mode):
+    """Instances of one sample_space grid; Philox streams stream0, stream0+1, ...
+    in (mu_a, mu_s', repeat, sphere) order, so a grid run alone or inside a
+    larger batch gives the same tallies."""
+    musr = np.asarray(mu_s_reduced, dtype=float)
+    mus = musr / (1 - g) if g != 1 else musr          # lookup.py:236
+    thr = 1e-3 if slides is None else 1e-4
+    sp_R = Spheres(**{**spheres.__dict__, "T": False})
+    sp_T = Spheres(**{**spheres.__dict__, "R": False})
+    insts, index = [], []
+    stream = stream0
+    for i, a in enumerate(np.asarray(mu_a, dtype=float)):
+        for j, s in enumerate(mus):
+            layers = _slab(n, float(a), float(s), g, t, slides)
+            for r in range(runs):
+                kinds = (("R", sp_R), ("T", sp_T)) if separate else (("RT", spheres),)
+                for which, sp in kinds:
+                    insts.append(make_instance(layers, sp, N, seed=seed, stream=stream,
+                                               mode=mode, roulette_threshold=thr))
+                    index.append((i, j, r, which))
+                    stream += 1
+    return insts, index
+
+
+def _grid_tables(res, index, shape):
+    Rd = np.zeros(shape)
+    Td = np.zeros(shape)
+    for (i, j, r, which), x in zip(index, res):
+        if which in ("R", "RT"):
+            Rd[i, j, r] = x.mean[1]
+        if which in ("T", "RT"):
+            Td[i, j, r] = x.mean[3]
+    return Rd, Td
 
 
 def sample_space(mu_a, mu_s_reduced, g, t, n, spheres: Spheres, N, runs=1, separate=True,
@@ -30,35 +69,148 @@ def sample_space(mu_a, mu_s_reduced, g, t, n, spheres: Spheres, N, runs=1, separ
     as lookup.py's pythonISMC), or a (top, bottom) pair of Layer slides
     (multilayer walk, roulette 1e-4, as ISMLMC.py)."""
     eng = engine or default_engine()
-    mu_a = np.asarray(mu_a, dtype=float)
-    musr = np.asarray(mu_s_reduced, dtype=float)
-    mus = musr / (1 - g) if g != 1 else musr          # lookup.py:236
-    thr = 1e-3 if slides is None else 1e-4
-    sp_R = Spheres(**{**spheres.__dict__, "T": False})
-    sp_T = Spheres(**{**spheres.__dict__, "R": False})
-    insts, index = [], []
-    stream = 0
-    for i, a in enumerate(mu_a):
-        for j, s in enumerate(mus):
-            layers = _slab(n, float(a), float(s), g, t, slides)
-            for r in range(runs):
-                if separate:
-                    for which, sp in (("R", sp_R), ("T", sp_T)):
-                        insts.append(make_instance(layers, sp, N, seed=seed, stream=stream,
-                                                   mode=mode, roulette_threshold=thr))
-                        index.append((i, j, r, which))
-                        stream += 1
-                else:
-                    insts.append(make_instance(layers, spheres, N, seed=seed, stream=stream,
-                                               mode=mode, roulette_threshold=thr))
-                    index.append((i, j, r, "RT"))
-                    stream += 1
-    res = eng.run_batch(insts, tune)
-    Rd = np.zeros((len(mu_a), len(mus), runs))
-    Td = np.zeros((len(mu_a), len(mus), runs))
-    for (i, j, r, which), x in zip(index, res):
-        if which in ("R", "RT"):
-            Rd[i, j, r] = x.mean[1]
-        if which in ("T", "RT"):
-            Td[i, j, r] = x.mean[3]
+    insts, index = _grid_instances(mu_a, mu_s_reduced, g, t, n, spheres, N, runs, separate, seed,
+                                   0, slides, mode)
+    Rd, Td = _grid_tables(eng.run_batch(insts, tune), index,
+                          (len(mu_a), len(mu_s_reduced), runs))
     return Rd.mean(-1), Rd.std(-1), Td.mean(-1), Td.std(-1)
+
+
+SPHERE_KEYS = ("R_pw", "R_fs", "R_fp", "R_fd", "R_angle", "T_pw", "T_fs", "T_fp", "T_fd", "T_angle")
+
+
+def sample_distributions(n, n_unc, spheres: Spheres, spheres_unc: dict, O, seed=0):
+    """O draws of the refractive index and of the sphere parameters from normal
+    distributions (lookup.py:133-143, minimization.py:132-152); spheres_unc
+    maps parameter names (SPHERE_KEYS) to standard deviations.  Total port
+    fractions follow their parts."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n_dist = rng.normal(n, n_unc, O)
+    draws = {k: rng.normal(getattr(spheres, k), spheres_unc.get(k, 0.0), O) for k in SPHERE_KEYS}
+    out = []
+    for r in range(O):
+        d = {**spheres.__dict__, **{k: float(v[r]) for k, v in draws.items()}}
+        d["R_f"] = d["R_fs"] + d["R_fp"] + d["R_fd"]
+        d["T_f"] = d["T_fs"] + d["T_fp"] + d["T_fd"]
+        out.append((float(n_dist[r]), Spheres(**d)))
+    return out
+
+
+def run_uncertainty(mu_a, mu_s_reduced, g, t, samples, N, runs=1, separate=True, seed=0,
+                    slides=None, mode="compat", engine=None, tune=None):
+    """lookup.py:263-293 (runPYTHON) as ONE launch: for every drawn (n, spheres)
+    in `samples` the whole grid with `runs` repeats.  Returns the mean over
+    samples of R_d and T_d and their spread: sqrt(sum of per-sample repeat
+    variances) when runs > 1, else the standard deviation over samples."""
+    eng = engine or default_engine()
+    insts, index, slices = [], [], []
+    per = len(mu_a) * len(mu_s_reduced) * runs * (2 if separate else 1)
+    for r, (n_r, sph_r) in enumerate(samples):
+        a, b = _grid_instances(mu_a, mu_s_reduced, g, t, n_r, sph_r, N, runs, separate, seed,
+                               r * per, slides, mode)
+        slices.append((len(insts), len(insts) + len(a)))
+        insts += a
+        index += b
+    res = eng.run_batch(insts, tune)
+    O = len(samples)
+    shape = (len(mu_a), len(mu_s_reduced), runs)
+    Rd, Td = np.zeros((O,) + shape[:2]), np.zeros((O,) + shape[:2])
+    Rv, Tv = np.zeros(shape[:2]), np.zeros(shape[:2])
+    for r, (lo, hi) in enumerate(slices):
+        R3, T3 = _grid_tables(res[lo:hi], index[lo:hi], shape)
+        Rd[r], Td[r] = R3.mean(-1), T3.mean(-1)
+        Rv += R3.std(-1) ** 2
+        Tv += T3.std(-1) ** 2
+    if runs > 1:
+        Rs, Ts = np.sqrt(Rv), np.sqrt(Tv)
+    else:
+        Rs, Ts = Rd.std(0), Td.std(0)
+    return Rd.mean(0), Rs, Td.mean(0), Ts
+
+
+# ----------------------------------------------------------------------------
+# lookup-table inversion on the GPU (Lookup/lookup.py:301-489)
+# ----------------------------------------------------------------------------
+def _dp(a):
+    return np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _rc(rc):
+    if rc:
+        buf = C.create_string_buffer(512)
+        load_library().ismc_last_error(None, buf, 512)
+        raise IsmcError(rc, buf.value.decode(errors="replace"))
+
+
+def table_grid(N):
+    """The table axis in percent: np.linspace(0, 100, N) (lookup.py:347-348)."""
+    return np.linspace(0, 100, N)
+
+
+def interp_table(R, T, values, N=1000, tri=None):
+    """Scattered samples (R, T in percent, value) -> N x N table indexed [R_i][T_j],
+    linear interpolation over a Delaunay triangulation (scipy.spatial, as
+    scipy.interpolate.griddata builds it), NaN outside the hull."""
+    R = np.ascontiguousarray(R, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.float64)
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    if tri is None:
+        from scipy.spatial import Delaunay
+        tri = Delaunay(np.stack([R, T], 1)).simplices
+    tri = np.ascontiguousarray(tri, dtype=np.int32)
+    out = np.empty((N, N))
+    _rc(load_library().ismc_table_interp(_dp(R), _dp(T), _dp(v), len(R),
+                                         tri.ctypes.data_as(C.POINTER(C.c_int32)), len(tri), N,
+                                         out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out
+
+
+def uncertainty_map(mua_table, mus_table, rstd_table, tstd_table, M=100, seed=0):
+    """Per-cell percent uncertainty of the mu_a and mu_s' tables from M Gaussian
+    draws of (R, T) (lookup.py:349-376); tables [R_i][T_j]."""
+    N = mua_table.shape[0]
+    a, b = np.empty((N, N)), np.empty((N, N))
+    _rc(load_library().ismc_table_uncertainty(_dp(mua_table), _dp(mus_table), _dp(rstd_table),
+                                              _dp(tstd_table), N, int(M), int(seed),
+                                              a.ctypes.data_as(C.POINTER(C.c_double)),
+                                              b.ctypes.data_as(C.POINTER(C.c_double))))
+    return a, b
+
+
+def lookup(table_t, R, T):
+    """Nearest-cell values of the transposed table table_t[T_j][R_i] for arrays of
+    measurements R, T in percent (lookup.py:467-489, vectorised)."""
+    N = table_t.shape[0]
+    R = np.atleast_1d(np.asarray(R, dtype=np.float64))
+    T = np.atleast_1d(np.asarray(T, dtype=np.float64))
+    out = np.empty(len(R))
+    _rc(load_library().ismc_table_lookup(_dp(table_t), N, _dp(R), _dp(T), len(R),
+                                         out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out
+
+
+def make_lookup(refl, trans, refl_std, trans_std, mu_a, mu_s_reduced, N=1000, uncertainty=True,
+                M=100, seed=0, skip_first=True):
+    """lookup.py:301-465 `makelookup` on the GPU (linear interpolation): the
+    (R, T) -> mu_a and mu_s' tables, the interpolated R/T standard deviations
+    and the uncertainty maps.  The reference skips the first row and column
+    of the grid (lookup.py:307-310); skip_first keeps that.  Returns the
+    transposed tables as the reference does: (mua_t, mua_unc_t, mus_t,
+    mus_unc_t, Rvals, Tvals)."""
+    refl, trans = np.asarray(refl, float), np.asarray(trans, float)
+    s = 1 if skip_first else 0
+    I, J = np.meshgrid(np.arange(s, refl.shape[0]), np.arange(s, refl.shape[1]), indexing="ij")
+    R = 100 * refl[I, J].ravel()
+    T = 100 * trans[I, J].ravel()
+    from scipy.spatial import Delaunay
+    tri = Delaunay(np.stack([R, T], 1)).simplices
+    mua_t = interp_table(R, T, np.asarray(mu_a, float)[I].ravel(), N, tri)
+    mus_t = interp_table(R, T, np.asarray(mu_s_reduced, float)[J].ravel(), N, tri)
+    if uncertainty:
+        rs = interp_table(R, T, 100 * np.asarray(refl_std, float)[I, J].ravel(), N, tri)
+        ts = interp_table(R, T, 100 * np.asarray(trans_std, float)[I, J].ravel(), N, tri)
+        ua, us = uncertainty_map(mua_t, mus_t, rs, ts, M, seed)
+    else:
+        ua = us = np.full((N, N), np.nan)
+    grid = table_grid(N)
+    return mua_t.T, ua.T, mus_t.T, us.T, grid, grid

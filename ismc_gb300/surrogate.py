@@ -116,6 +116,8 @@ class Surrogate:
             a = t.as_tensor(np.asarray(a, dtype=np.float32))
         a = a.to(device=f"cuda:{self.device}", dtype=t.float32).contiguous()
         assert a.ndim == 2 and a.shape[1] == cols
+        # the library's stream must not read before torch's producer finished
+        t.cuda.current_stream(a.device).synchronize()
         return a
 
     def forward(self, x):
@@ -167,17 +169,16 @@ class Surrogate:
         for ep in range(epochs):
             perm = t.randperm(X.shape[0], generator=g, device=X.device)[:n]
             Xs, Ys = X[perm].contiguous(), Y[perm].contiguous()
-            losses = []
-            for b in range(steps_per_epoch):
-                cur = 0.5 * lr * (1 + math.cos(math.pi * step / total))
-                want = (b == steps_per_epoch - 1) or (log_every and b % log_every == 0)
-                l = self.train_step(Xs[b * batch:(b + 1) * batch], Ys[b * batch:(b + 1) * batch],
-                                    cur, want_loss=want)
-                if want:
-                    losses.append(l)
-                step += 1
-            hist.append(float(np.mean(losses)))
-        self._check(self.lib.ismc_mlp_sync(self.h))
+            t.cuda.current_stream(X.device).synchronize()       # gather done before use
+            lrs = np.array([0.5 * lr * (1 + math.cos(math.pi * (step + b) / total))
+                            for b in range(steps_per_epoch)], dtype=np.float32)
+            loss = C.c_float()
+            # the whole epoch in one native call: no per-step Python
+            self._check(self.lib.ismc_mlp_train_epoch(
+                self.h, Xs.data_ptr(), Ys.data_ptr(), n, batch,
+                lrs.ctypes.data_as(C.POINTER(C.c_float)), C.byref(loss)))
+            step += steps_per_epoch
+            hist.append(float(loss.value))
         return hist
 
 
@@ -191,68 +192,132 @@ def _grid(nmua=48, nmus=48):
     return np.stack([A.ravel(), S.ravel()], 1)
 
 
-def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=8, verify_packets=1_000_000,
-                    seed=7, fallback=True, plain_packets=100_000, plain_max_evals=400):
-    """Solve many measurements [m x 3] of (R_d, T_d, T_u) with noise sigma (3,).
-
-    Returns dict with x [m x 2] (mu_a, mu_s'), verified MC values, fallback mask,
-    and timings of each phase."""
-    import torch
-    meas = np.asarray(meas, dtype=np.float64)
-    sig = np.asarray(sigma, dtype=np.float64)
-    m = len(meas)
-    T = {}
-    t0 = time.perf_counter()
-    # (1) grid proposal: surrogate on a 48 x 48 (ln mu_a, ln mu_s') grid, shared by all
-    grid = _grid()
-    X = np.concatenate([grid, np.tile([g, d, n], (len(grid), 1))], 1)
-    out = sur.forward(X).cpu().numpy()[:, :3].astype(np.float64)
-    mt = torch.as_tensor(meas, device="cuda")
-    ot = torch.as_tensor(out, device="cuda")
-    st = torch.as_tensor(sig, device="cuda")
-    best = []
-    for a in range(0, m, 2048):
-        r = (((ot[None, :, :] - mt[a:a + 2048, None, :]) / st) ** 2).sum(-1)
-        best.append(r.argmin(1).cpu().numpy())
-    x = grid[np.concatenate(best)].copy()
-    T["propose_s"] = time.perf_counter() - t0
-    # (2) Gauss-Newton on the surrogate (forward differences, damped)
-    t1 = time.perf_counter()
-    h = 1e-3
-    for _ in range(gn_steps):
-        pts = np.concatenate([x, x + [h, 0.0], x + [0.0, h]], 0)
+def _gauss_newton(sur, x, meas, w, offset, steps, g, d, n, h=0.05):
+    """Damped Gauss-Newton on the surrogate for rows x [m x 2] (ln mu_a, ln mu_s'):
+    minimise sum_k (w_k (meas_k - f_k(x) - offset_k))^2 with central
+    differences of step h (the network is piecewise smooth at bf16 activation
+    resolution, so the step is kept well above it).  w is [m x 3] or [3]."""
+    w = np.broadcast_to(np.asarray(w, dtype=np.float64), meas.shape)
+    m = len(x)
+    for _ in range(steps):
+        pts = np.concatenate([x, x + [h, 0.0], x - [h, 0.0], x + [0.0, h], x - [0.0, h]], 0)
         Xp = np.concatenate([pts, np.tile([g, d, n], (len(pts), 1))], 1)
         o = sur.forward(Xp).cpu().numpy()[:, :3].astype(np.float64)
-        f0, fa, fs = o[:m], o[m:2 * m], o[2 * m:]
-        J = np.stack([(fa - f0) / h, (fs - f0) / h], 2) / sig[None, :, None]     # m x 3 x 2
-        rsd = (meas - f0) / sig                                                   # m x 3
-        JtJ = np.einsum("mki,mkj->mij", J, J) + 1e-6 * np.eye(2)
+        f0 = o[:m] + offset
+        J = np.stack([(o[m:2 * m] - o[2 * m:3 * m]) / (2 * h),
+                      (o[3 * m:4 * m] - o[4 * m:]) / (2 * h)], 2) * w[:, :, None]   # m x 3 x 2
+        rsd = (meas - f0) * w                                                         # m x 3
+        JtJ = np.einsum("mki,mkj->mij", J, J)
+        JtJ = JtJ + (1e-3 * np.trace(JtJ, axis1=1, axis2=2)[:, None, None] + 1e-9) * np.eye(2)
         Jtr = np.einsum("mki,mk->mi", J, rsd)
         dx = np.linalg.solve(JtJ, Jtr[..., None])[..., 0]
-        dx = np.clip(dx, -1.0, 1.0)
+        dx = np.clip(dx, -0.5, 0.5)
         x = np.clip(x + dx, LO[:2], HI[:2])
-    T["gauss_newton_s"] = time.perf_counter() - t1
-    # (3) Monte Carlo verification at the answers: one batched launch
-    t2 = time.perf_counter()
+    return x
+
+
+def _verify(engine, x, g, d, n, packets, seed, stream0=0):
     sph = bench_spheres()
     insts = [make_instance(sample_stack(math.exp(x[i, 0]), math.exp(x[i, 1]), g, d, n), sph,
-                           verify_packets, seed=seed, stream=i) for i in range(m)]
+                           packets, seed=seed, stream=stream0 + i) for i in range(len(x))]
     res = engine.run_batch(insts)
     V = np.array([[r.mean[1], r.mean[3], r.mean[4]] for r in res])
     VS = np.array([[r.se[1], r.se[3], r.se[4]] for r in res])
+    return V, VS
+
+
+def objective_weights(meas, sigma, objective="reference"):
+    """Per-measurement residual weights [m x 3] for (R_d, T_d, T_u).
+
+    "reference": the plain path's cost (minimization.py:231-238,
+    ISMLMC-minimization.cu:120-128): relative residuals of R_d and T_d,
+    absolute residual of T_u, so both paths solve the same problem;
+    "chi2": residuals in units of the measurement noise sigma."""
+    meas = np.asarray(meas, dtype=np.float64)
+    if objective == "chi2":
+        return np.broadcast_to(1.0 / np.asarray(sigma, dtype=np.float64), meas.shape).copy()
+    if objective != "reference":
+        raise ValueError(f"unknown objective {objective!r}")
+    w = np.ones_like(meas)
+    w[:, 0] = 1.0 / np.maximum(np.abs(meas[:, 0]), 1e-6)
+    w[:, 1] = 1.0 / np.maximum(np.abs(meas[:, 1]), 1e-6)
+    return w
+
+
+def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=10, verify_packets=1_000_000,
+                    seed=7, fallback=True, correct=True, plain_packets=100_000, plain_max_evals=400,
+                    objective="reference"):
+    """Solve many measurements [m x 3] of (R_d, T_d, T_u) with noise sigma (3,).
+
+    (1) The surrogate on a 48 x 48 (ln mu_a, ln mu_s') grid proposes a start;
+    (2) Gauss-Newton steps on the surrogate refine it; (3) one Monte Carlo run
+    of `verify_packets` checks it.  (3b) With `correct`, a solve that misses
+    by more than 3 sigma takes the Monte Carlo-minus-surrogate difference at
+    its point as an output offset, re-solves on the offset surrogate and is
+    verified again.  (4) What still misses falls back to the plain path
+    (PRAXIS on Monte Carlo).  Steps (1)-(3b) minimise `objective` (see
+    objective_weights); the 3-sigma test of the verification uses sigma.  Returns dict with x [m x 2] (mu_a, mu_s'), the
+    verified MC values, masks of corrected and fallback solves, and timings."""
+    import torch
+    meas = np.asarray(meas, dtype=np.float64)
+    sig = np.asarray(sigma, dtype=np.float64)
+    wts = objective_weights(meas, sig, objective)
+    m = len(meas)
+    T = {}
+    t0 = time.perf_counter()
+    # (1) grid proposal, shared surrogate evaluations for all measurements
+    grid = _grid()
+    X = np.concatenate([grid, np.tile([g, d, n], (len(grid), 1))], 1)
+    ot = sur.forward(X)[:, :3]
+    mt = torch.as_tensor(meas, device=ot.device, dtype=torch.float32)
+    wt = torch.as_tensor(wts, device=ot.device, dtype=torch.float32)
+    best = []
+    for a in range(0, m, 4096):
+        r = (((ot[None, :, :] - mt[a:a + 4096, None, :]) * wt[a:a + 4096, None, :]) ** 2).sum(-1)
+        best.append(r.argmin(1))
+    x = grid[torch.cat(best).cpu().numpy()].copy()
+    T["propose_s"] = time.perf_counter() - t0
+    # (2) Gauss-Newton on the surrogate
+    t1 = time.perf_counter()
+    x = _gauss_newton(sur, x, meas, wts, 0.0, gn_steps, g, d, n)
+    T["gauss_newton_s"] = time.perf_counter() - t1
+    # (3) Monte Carlo verification at the answers: one batched launch
+    t2 = time.perf_counter()
+    V, VS = _verify(engine, x, g, d, n, verify_packets, seed)
     T["verify_s"] = time.perf_counter() - t2
-    miss = np.any(np.abs(V - meas) > 3 * np.sqrt(sig ** 2 + VS ** 2), axis=1)
-    # (4) fallback to the plain path for the misses
+
+    def missed(V, VS):
+        return np.any(np.abs(V - meas) > 3 * np.sqrt(sig ** 2 + VS ** 2), axis=1)
+
+    miss = missed(V, VS)
+    corrected = np.zeros(m, dtype=bool)
+    # (3b) offset correction of the misses, verified again
     t3 = time.perf_counter()
+    if correct and miss.any():
+        idx = np.nonzero(miss)[0]
+        xi = x[idx]
+        Xi = np.concatenate([xi, np.tile([g, d, n], (len(xi), 1))], 1)
+        off = V[idx] - sur.forward(Xi).cpu().numpy()[:, :3].astype(np.float64)
+        xi = _gauss_newton(sur, xi, meas[idx], wts[idx], off, gn_steps, g, d, n)
+        Vi, VSi = _verify(engine, xi, g, d, n, verify_packets, seed + 1, stream0=m)
+        x[idx], V[idx], VS[idx] = xi, Vi, VSi
+        corrected[idx] = True
+        miss = missed(V, VS)
+    T["correct_s"] = time.perf_counter() - t3
+    # (4) fallback to the plain path for what still misses
+    t4 = time.perf_counter()
     xr = np.exp(x)
     if fallback and miss.any():
         idx = np.nonzero(miss)[0]
+        sph = bench_spheres()
         reqs = [make_solve(sample_stack(1.0, 10.0, g, d, n), 1, sph, plain_packets,
                            (meas[i, 0], None, meas[i, 1], meas[i, 2]), x0=tuple(xr[i]),
-                           seed=seed + 1, max_evals=plain_max_evals) for i in idx]
+                           seed=seed + 1, lo=(0.005, 0.5), hi=(20.0, 200.0),
+                           max_evals=plain_max_evals) for i in idx]
         outp = engine.solve_batch(reqs)
         for i, o in zip(idx, outp):
             xr[i] = (o.x[0], o.x[1])
-    T["fallback_s"] = time.perf_counter() - t3
+    T["fallback_s"] = time.perf_counter() - t4
     T["total_s"] = time.perf_counter() - t0
-    return {"x": xr, "verified": V, "verified_se": VS, "fallback": miss, "timing": T}
+    return {"x": xr, "verified": V, "verified_se": VS, "corrected": corrected, "fallback": miss,
+            "timing": T}

@@ -3,12 +3,15 @@ surrogate MLP, for checking the tensor-core kernels' outputs and gradients.
 
 Network: x (5 raw inputs) -> map each feature to [-1, 1] -> 256 -> 256 -> 256
 -> 6 with SiLU hidden activations.  Outputs: mu (3) and log-variance s (3).
-Loss: mean over rows of sum_k 0.5 * (exp(-s_k) (y_k - mu_k)^2 + s_k).
+Loss: mean over rows of sum_k 0.5 * ((y_k - mu_k)^2 / v_k + ln v_k),
+v_k = exp(s_k) + floor^2 (Gaussian NLL with a variance floor).
 
 With bf16=True the oracle rounds to bfloat16 exactly where the GPU path stores
 bfloat16 (weights, normalised inputs, hidden activations, SiLU derivatives,
 output gradient, back-propagated gradients), and otherwise computes in FP64,
-so the remaining difference is only the FP32 accumulation order.
+so the remaining difference is only the FP32 accumulation order.  Each
+normalised input f enters the first layer as bf16(f) + bf16(f - bf16(f)), the
+two bf16 columns the GPU path stores for it.
 """
 import numpy as np
 
@@ -48,7 +51,9 @@ def _sig(z):
 
 def forward(params, x, rnd=lambda a: a):
     layers = unflatten(params)
-    h = rnd(2.0 * (np.asarray(x, dtype=np.float64) - LO) / (HI - LO) - 1.0)
+    f = 2.0 * (np.asarray(x, dtype=np.float64) - LO) / (HI - LO) - 1.0
+    hi = rnd(f)
+    h = hi + rnd(f - hi)
     acts, gates = [h], []
     for W, b in layers[:3]:
         z = h @ rnd(W).T + b
@@ -61,7 +66,12 @@ def forward(params, x, rnd=lambda a: a):
     return out, acts, gates
 
 
-def loss_and_grad(params, x, y, bf16_emulation=False):
+VAR_FLOOR = 3e-4      # standard-deviation floor of the loss (the GPU kernel's kVarFloor)
+
+
+def loss_and_grad(params, x, y, bf16_emulation=False, floor=VAR_FLOOR):
+    """Gaussian NLL with variance v = exp(s) + floor^2:
+    mean over rows of sum_k 0.5 (d^2 / v + ln v), d = y - mu."""
     rnd = bf16 if bf16_emulation else (lambda a: a)
     layers = unflatten(params)
     out, acts, gates = forward(params, x, rnd)
@@ -69,9 +79,10 @@ def loss_and_grad(params, x, y, bf16_emulation=False):
     B = out.shape[0]
     mu, s = out[:, :3], out[:, 3:6]
     d = y - mu
-    ie = np.exp(-s)
-    loss = np.mean(np.sum(0.5 * (ie * d * d + s), axis=1))
-    dout = np.concatenate([-ie * d, 0.5 * (1 - ie * d * d)], axis=1) / B
+    es = np.exp(s)
+    v = es + floor * floor
+    loss = np.mean(np.sum(0.5 * (d * d / v + np.log(v)), axis=1))
+    dout = np.concatenate([-d / v, 0.5 * (es / v) * (1 - d * d / v)], axis=1) / B
     dout = rnd(dout)
     grads = [None] * 4
     W4, _ = layers[3]

@@ -70,6 +70,38 @@ def test_mlp_forward_matches_oracle(sur):
     assert np.max(np.abs(out - ref[:, :6])) < 2e-2 * max(1.0, np.max(np.abs(ref)))
 
 
+def test_adam_trajectory_tracks_fp64_oracle():
+    """20 Adam steps on the GPU move the parameters the way 20 FP64 Adam steps
+    on the oracle's gradients (with bf16 emulation) do."""
+    import torch
+    from oracle import mlp64
+    from ismc_gb300.surrogate import Surrogate
+    s = Surrogate(0, max_batch=512, seed=21)
+    try:
+        rng = np.random.default_rng(7)
+        x = (mlp64.LO + (mlp64.HI - mlp64.LO) * rng.random((512, 5))).astype(np.float32)
+        y = (rng.random((512, 3)) * [0.5, 0.3, 0.2]).astype(np.float32)
+        dx, dy = torch.as_tensor(x).cuda(), torch.as_tensor(y).cuda()
+        p0 = s.get_params().astype(np.float64)
+        lr, steps = 1e-3, 20
+        for _ in range(steps):
+            s.train_step(dx, dy, lr)
+        p_gpu = s.get_params().astype(np.float64)
+        p, m, v = p0.copy(), np.zeros_like(p0), np.zeros_like(p0)
+        x64, y64 = x.astype(np.float64), y.astype(np.float64)
+        for t in range(1, steps + 1):
+            _, g = mlp64.loss_and_grad(p.astype(np.float32).astype(np.float64), x64, y64,
+                                       bf16_emulation=True)
+            m = 0.9 * m + 0.1 * g
+            v = 0.999 * v + 0.001 * g * g
+            p = p - lr * (m / (1 - 0.9 ** t)) / (np.sqrt(v / (1 - 0.999 ** t)) + 1e-8)
+        du_gpu, du_ref = p_gpu - p0, p - p0
+        rel = np.linalg.norm(du_gpu - du_ref) / np.linalg.norm(du_ref)
+        assert rel < 0.1, rel
+    finally:
+        s.close()
+
+
 def test_mlp_training_lowers_loss():
     """Fit a smooth synthetic map (stand-in targets; the Monte Carlo data path is
     exercised by the surrogate-solve test): the loss must fall well below its start."""
