@@ -296,6 +296,16 @@ int ismc_mlp_last_error(const ismc_mlp* m, char* buf, size_t n);
  *   ismc_table_interp: linear interpolation of scattered samples (R, T, value)
  *     onto the table over the caller's triangulation tri[ntri][3] (Delaunay,
  *     as scipy.interpolate.griddata builds it, lookup.py:341-345); NaN outside.
+ *   ismc_table_interp_cubic: the same table by Clough-Tocher cubic
+ *     interpolation, the method griddata(method="cubic") applies in
+ *     lookup.py:339-342.  nbr[ntri][3] holds the triangle across the edge
+ *     opposite each vertex (-1 on the hull), as scipy.spatial.Delaunay's
+ *     `neighbors`.  adj_ptr[npts+1] / adj is the vertex adjacency in CSR form
+ *     (scipy's `vertex_neighbor_vertices`); pass NULL for both to derive it
+ *     from the triangles.  Vertex gradients come from the global
+ *     curvature-minimising estimate (Gauss-Seidel, tolerance 1e-6, at most
+ *     400 sweeps) on the host; the per-cell cubic patches are evaluated on
+ *     the GPU.
  *   ismc_table_uncertainty: lookup.py:349-376 -- per cell with finite,
  *     non-negative standard deviations, M normal draws of (R, T), nearest-cell
  *     values of both tables, 100 * std / value; NaN elsewhere.
@@ -304,6 +314,9 @@ int ismc_mlp_last_error(const ismc_mlp* m, char* buf, size_t n);
  * ------------------------------------------------------------------------ */
 int ismc_table_interp(const double* R, const double* T, const double* val, uint32_t npts,
                       const int32_t* tri, uint32_t ntri, uint32_t N, double* out);
+int ismc_table_interp_cubic(const double* R, const double* T, const double* val, uint32_t npts,
+                            const int32_t* tri, const int32_t* nbr, uint32_t ntri,
+                            const int32_t* adj_ptr, const int32_t* adj, uint32_t N, double* out);
 int ismc_table_uncertainty(const double* mua, const double* mus, const double* rstd,
                            const double* tstd, uint32_t N, uint32_t M, uint64_t seed,
                            double* mua_unc, double* mus_unc);

@@ -85,7 +85,8 @@ EXPORTS = ("ismc_version", "ismc_init", "ismc_destroy", "ismc_run", "ismc_run_ba
            "ismc_mlp_create", "ismc_mlp_destroy", "ismc_mlp_nparam", "ismc_mlp_get_params",
            "ismc_mlp_set_params", "ismc_mlp_forward", "ismc_mlp_grad", "ismc_mlp_train_step",
            "ismc_mlp_sync", "ismc_mlp_gemm_test", "ismc_mlp_last_error", "ismc_mlp_train_epoch",
-           "ismc_table_interp", "ismc_table_uncertainty", "ismc_table_lookup")
+           "ismc_table_interp", "ismc_table_interp_cubic", "ismc_table_uncertainty",
+           "ismc_table_lookup")
 
 NOALLOC_MAX_INST = 1024
 
@@ -146,6 +147,9 @@ def declare(lib):
     D = P(C.c_double)
     lib.ismc_table_interp.restype = C.c_int
     lib.ismc_table_interp.argtypes = [D, D, D, C.c_uint32, P(C.c_int32), C.c_uint32, C.c_uint32, D]
+    lib.ismc_table_interp_cubic.restype = C.c_int
+    lib.ismc_table_interp_cubic.argtypes = [D, D, D, C.c_uint32, P(C.c_int32), P(C.c_int32),
+                                            C.c_uint32, P(C.c_int32), P(C.c_int32), C.c_uint32, D]
     lib.ismc_table_uncertainty.restype = C.c_int
     lib.ismc_table_uncertainty.argtypes = [D, D, D, D, C.c_uint32, C.c_uint32, C.c_uint64, D, D]
     lib.ismc_table_lookup.restype = C.c_int

@@ -22,7 +22,7 @@ The driver file is read, patched in memory (never on disk) and executed as
     an .npz file beside the requested .h5 name);
   * with gpu_tables, lookup.py's makelookup (cubic griddata and a Python
     Monte Carlo uncertainty loop) is replaced by ismc_gb300.lookup.make_lookup
-    (GPU, linear interpolation on the same triangulation).
+    (the same Clough-Tocher interpolation and uncertainty map on the GPU).
 
 Every patch asserts that the text it replaces is present, so a driver of a
 different version fails loudly instead of running half-patched.

@@ -147,21 +147,36 @@ def table_grid(N):
     return np.linspace(0, 100, N)
 
 
-def interp_table(R, T, values, N=1000, tri=None):
+def _i32p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def interp_table(R, T, values, N=1000, tri=None, method="cubic"):
     """Scattered samples (R, T in percent, value) -> N x N table indexed [R_i][T_j],
-    linear interpolation over a Delaunay triangulation (scipy.spatial, as
-    scipy.interpolate.griddata builds it), NaN outside the hull."""
+    NaN outside the samples' convex hull, as scipy.interpolate.griddata makes it
+    (lookup.py:339-342).  method "cubic" (Clough-Tocher, griddata's cubic) or
+    "linear" (barycentric).  tri: a scipy.spatial.Delaunay of the points (built
+    here when None; for "linear" an [ntri x 3] simplex array also works)."""
     R = np.ascontiguousarray(R, dtype=np.float64)
     T = np.ascontiguousarray(T, dtype=np.float64)
     v = np.ascontiguousarray(values, dtype=np.float64)
     if tri is None:
         from scipy.spatial import Delaunay
-        tri = Delaunay(np.stack([R, T], 1)).simplices
-    tri = np.ascontiguousarray(tri, dtype=np.int32)
+        tri = Delaunay(np.stack([R, T], 1))
     out = np.empty((N, N))
-    _rc(load_library().ismc_table_interp(_dp(R), _dp(T), _dp(v), len(R),
-                                         tri.ctypes.data_as(C.POINTER(C.c_int32)), len(tri), N,
-                                         out.ctypes.data_as(C.POINTER(C.c_double))))
+    optr = out.ctypes.data_as(C.POINTER(C.c_double))
+    lib = load_library()
+    if method == "linear":
+        simp = np.ascontiguousarray(getattr(tri, "simplices", tri), dtype=np.int32)
+        _rc(lib.ismc_table_interp(_dp(R), _dp(T), _dp(v), len(R), _i32p(simp), len(simp), N, optr))
+    elif method == "cubic":
+        simp = np.ascontiguousarray(tri.simplices, dtype=np.int32)
+        nbr = np.ascontiguousarray(tri.neighbors, dtype=np.int32)
+        ptr, adj = (np.ascontiguousarray(a, dtype=np.int32) for a in tri.vertex_neighbor_vertices)
+        _rc(lib.ismc_table_interp_cubic(_dp(R), _dp(T), _dp(v), len(R), _i32p(simp), _i32p(nbr),
+                                        len(simp), _i32p(ptr), _i32p(adj), N, optr))
+    else:
+        raise ValueError(f"method must be 'cubic' or 'linear', not {method!r}")
     return out
 
 
@@ -190,25 +205,28 @@ def lookup(table_t, R, T):
 
 
 def make_lookup(refl, trans, refl_std, trans_std, mu_a, mu_s_reduced, N=1000, uncertainty=True,
-                M=100, seed=0, skip_first=True):
-    """lookup.py:301-465 `makelookup` on the GPU (linear interpolation): the
-    (R, T) -> mu_a and mu_s' tables, the interpolated R/T standard deviations
-    and the uncertainty maps.  The reference skips the first row and column
-    of the grid (lookup.py:307-310); skip_first keeps that.  Returns the
-    transposed tables as the reference does: (mua_t, mua_unc_t, mus_t,
-    mus_unc_t, Rvals, Tvals)."""
+                M=100, seed=0, skip_first=True, method="cubic"):
+    """lookup.py:301-465 `makelookup` on the GPU: the (R, T) -> mu_a and mu_s'
+    tables, the interpolated R/T standard deviations and the uncertainty maps.
+    As the reference does, the first row and column of the grid are skipped
+    (lookup.py:307-310; skip_first), the samples are ordered by R then T
+    (lookup.py:320-323) and interpolated with griddata's method (cubic by
+    default).  Returns the transposed tables as the reference does: (mua_t,
+    mua_unc_t, mus_t, mus_unc_t, Rvals, Tvals)."""
     refl, trans = np.asarray(refl, float), np.asarray(trans, float)
     s = 1 if skip_first else 0
     I, J = np.meshgrid(np.arange(s, refl.shape[0]), np.arange(s, refl.shape[1]), indexing="ij")
     R = 100 * refl[I, J].ravel()
     T = 100 * trans[I, J].ravel()
+    order = np.lexsort((T, R))          # stable sort by R, then T
+    R, T, I, J = R[order], T[order], I.ravel()[order], J.ravel()[order]
     from scipy.spatial import Delaunay
-    tri = Delaunay(np.stack([R, T], 1)).simplices
-    mua_t = interp_table(R, T, np.asarray(mu_a, float)[I].ravel(), N, tri)
-    mus_t = interp_table(R, T, np.asarray(mu_s_reduced, float)[J].ravel(), N, tri)
+    tri = Delaunay(np.stack([R, T], 1))
+    mua_t = interp_table(R, T, np.asarray(mu_a, float)[I], N, tri, method)
+    mus_t = interp_table(R, T, np.asarray(mu_s_reduced, float)[J], N, tri, method)
     if uncertainty:
-        rs = interp_table(R, T, 100 * np.asarray(refl_std, float)[I, J].ravel(), N, tri)
-        ts = interp_table(R, T, 100 * np.asarray(trans_std, float)[I, J].ravel(), N, tri)
+        rs = interp_table(R, T, 100 * np.asarray(refl_std, float)[I, J], N, tri, method)
+        ts = interp_table(R, T, 100 * np.asarray(trans_std, float)[I, J], N, tri, method)
         ua, us = uncertainty_map(mua_t, mus_t, rs, ts, M, seed)
     else:
         ua = us = np.full((N, N), np.nan)

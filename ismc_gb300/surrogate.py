@@ -317,7 +317,12 @@ def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=10, 
         outp = engine.solve_batch(reqs)
         for i, o in zip(idx, outp):
             xr[i] = (o.x[0], o.x[1])
+        fallback_evals = sum(int(o.evals) for o in outp)
+    else:
+        fallback_evals = 0
     T["fallback_s"] = time.perf_counter() - t4
     T["total_s"] = time.perf_counter() - t0
+    # Monte Carlo packets spent: verification, re-verification, fallback objectives
+    mc = (m + int(corrected.sum())) * verify_packets + fallback_evals * plain_packets
     return {"x": xr, "verified": V, "verified_se": VS, "corrected": corrected, "fallback": miss,
-            "timing": T}
+            "timing": T, "mc_packets": mc, "fallback_evals": fallback_evals}

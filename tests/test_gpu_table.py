@@ -1,5 +1,6 @@
-"""Lookup-table inversion on the GPU (Lookup/lookup.py:301-489): linear
-interpolation against scipy's griddata on the same triangulation, the Monte
+"""Lookup-table inversion on the GPU (Lookup/lookup.py:301-489): cubic
+(Clough-Tocher) and linear interpolation against scipy's griddata on the same
+triangulation, the cubic one also against the FP64 restatement, the Monte
 Carlo uncertainty map against the FP64 numpy restatement with the same normal
 draws (oracle/table64.py), and the nearest-cell lookup."""
 import numpy as np
@@ -24,7 +25,7 @@ def test_interp_matches_scipy_linear():
     R, T, v = _scattered()
     N = 301
     tri = Delaunay(np.stack([R, T], 1))
-    got = interp_table(R, T, v, N, tri.simplices)
+    got = interp_table(R, T, v, N, tri.simplices, method="linear")
     g = table_grid(N)
     gx, gy = np.meshgrid(g, g, indexing="ij")
     ref = griddata(np.stack([R, T], 1), v, (gx, gy), method="linear")
@@ -33,6 +34,49 @@ def test_interp_matches_scipy_linear():
     # NaN masks differ at most on cells lying on the hull boundary
     assert np.mean(np.isfinite(got) != np.isfinite(ref)) < 2e-3
     assert both.sum() > 0.05 * N * N          # the samples' hull covers ~10 % of the table
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_interp_cubic_matches_scipy_and_oracle(seed):
+    """griddata(method="cubic") is what lookup.py interpolates with: the GPU
+    Clough-Tocher table agrees with it, cell for cell, to rounding."""
+    from scipy.interpolate import griddata
+    from oracle import table64
+    from ismc_gb300.lookup import interp_table, table_grid
+    R, T, v = _scattered(n=30, seed=seed)
+    order = np.lexsort((T, R))
+    R, T, v = R[order], T[order], v[order]
+    N = 201
+    got = interp_table(R, T, v, N, method="cubic")
+    g = table_grid(N)
+    gx, gy = np.meshgrid(g, g, indexing="ij")
+    ref = griddata(np.stack([R, T], 1), v, (gx, gy), method="cubic")
+    both = np.isfinite(got) & np.isfinite(ref)
+    scale = np.max(np.abs(ref[both]))
+    assert np.max(np.abs(got[both] - ref[both])) < 1e-9 * scale
+    assert np.mean(np.isfinite(got) != np.isfinite(ref)) < 2e-3
+    assert both.sum() > 0.05 * N * N
+    if seed == 0:                      # the FP64 restatement on a coarser table
+        Nc = 41
+        oc = table64.cubic_table(R, T, v, Nc)
+        gc = interp_table(R, T, v, Nc, method="cubic")
+        bc = np.isfinite(oc) & np.isfinite(gc)
+        assert bc.sum() > 0 and np.max(np.abs(oc[bc] - gc[bc])) < 1e-9 * scale
+
+
+def test_interp_cubic_reproduces_linear_data():
+    """A linear function has zero curvature: the estimated gradients are exact
+    and the cubic table equals the function inside the hull."""
+    from ismc_gb300.lookup import interp_table, table_grid
+    R, T, _ = _scattered(n=20, seed=3)
+    v = 0.3 + 0.02 * R - 0.05 * T
+    N = 101
+    got = interp_table(R, T, v, N, method="cubic")
+    g = table_grid(N)
+    gx, gy = np.meshgrid(g, g, indexing="ij")
+    f = np.isfinite(got)
+    assert f.sum() > 0
+    assert np.max(np.abs(got[f] - (0.3 + 0.02 * gx[f] - 0.05 * gy[f]))) < 1e-10
 
 
 def test_uncertainty_map_matches_oracle():

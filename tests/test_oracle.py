@@ -243,3 +243,24 @@ def test_analytic64_closed_forms():
     a = math.exp(-float(np.float32(mu)) * float(np.float32(d)))
     _, ball = oracle.analytic64([n], [0.0], [mu], [d], mode="physical")
     assert abs(ball - (1 - r) ** 2 * a / (1 - r * r * a * a)) < 1e-12
+
+
+def test_cubic_table_oracle_matches_scipy_griddata():
+    """Pin of the Clough-Tocher restatement: scipy.interpolate.griddata(cubic),
+    the interpolation lookup.py:339-342 uses, on scattered data."""
+    import numpy as np
+    from scipy.interpolate import griddata
+    from oracle import table64
+    rng = np.random.default_rng(3)
+    R = rng.random(150) * 60 + 10
+    T = rng.random(150) * 40 + 5
+    v = np.exp(-R / 30) * (1 + T / 50)
+    N = 60
+    tab = table64.cubic_table(R, T, v, N)
+    g = np.linspace(0, 100, N)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    ref = griddata(np.stack([R, T], 1), v, (X, Y), method="cubic")
+    assert np.array_equal(np.isnan(ref), np.isnan(tab))
+    f = np.isfinite(ref)
+    assert f.sum() > 500
+    assert np.max(np.abs(ref[f] - tab[f])) < 1e-12
