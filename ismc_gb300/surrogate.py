@@ -226,13 +226,14 @@ def _verify(engine, x, g, d, n, packets, seed, stream0=0):
     return V, VS
 
 
-def objective_weights(meas, sigma, objective="reference"):
+def objective_weights(meas, sigma, objective="chi2"):
     """Per-measurement residual weights [m x 3] for (R_d, T_d, T_u).
 
+    "chi2": residuals in units of the measurement noise sigma, the same
+    weighting as the 3-sigma verification test;
     "reference": the plain path's cost (minimization.py:231-238,
     ISMLMC-minimization.cu:120-128): relative residuals of R_d and T_d,
-    absolute residual of T_u, so both paths solve the same problem;
-    "chi2": residuals in units of the measurement noise sigma."""
+    absolute residual of T_u."""
     meas = np.asarray(meas, dtype=np.float64)
     if objective == "chi2":
         return np.broadcast_to(1.0 / np.asarray(sigma, dtype=np.float64), meas.shape).copy()
@@ -246,7 +247,7 @@ def objective_weights(meas, sigma, objective="reference"):
 
 def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=10, verify_packets=1_000_000,
                     seed=7, fallback=True, correct=True, plain_packets=100_000, plain_max_evals=400,
-                    objective="reference"):
+                    objective="chi2"):
     """Solve many measurements [m x 3] of (R_d, T_d, T_u) with noise sigma (3,).
 
     (1) The surrogate on a 48 x 48 (ln mu_a, ln mu_s') grid proposes a start;

@@ -65,8 +65,9 @@ def test_interp_cubic_matches_scipy_and_oracle(seed):
 
 
 def test_interp_cubic_reproduces_linear_data():
-    """A linear function has zero curvature: the estimated gradients are exact
-    and the cubic table equals the function inside the hull."""
+    """A linear function has zero curvature: the gradient estimate converges to
+    the exact gradient and the cubic table equals the function inside the hull,
+    to the estimate's convergence tolerance (1e-6 relative change per sweep)."""
     from ismc_gb300.lookup import interp_table, table_grid
     R, T, _ = _scattered(n=20, seed=3)
     v = 0.3 + 0.02 * R - 0.05 * T
@@ -76,7 +77,7 @@ def test_interp_cubic_reproduces_linear_data():
     gx, gy = np.meshgrid(g, g, indexing="ij")
     f = np.isfinite(got)
     assert f.sum() > 0
-    assert np.max(np.abs(got[f] - (0.3 + 0.02 * gx[f] - 0.05 * gy[f]))) < 1e-10
+    assert np.max(np.abs(got[f] - (0.3 + 0.02 * gx[f] - 0.05 * gy[f]))) < 1e-6
 
 
 def test_uncertainty_map_matches_oracle():
