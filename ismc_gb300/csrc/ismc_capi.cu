@@ -33,7 +33,7 @@ struct ismc_ctx {
     ismc_tally* h_out = nullptr;
     // launch shape
     ismc_tune tune{256, 0, 0, 0};
-    uint32_t chunks_per_warp = 8;   // queue chunks per warp when sized on the device
+    uint32_t chunks_per_warp = 32;  // queue chunks per warp when sized on the device
     bool tuned = false;
     // graph of the host-pointer pipeline
     cudaGraphExec_t gexec = nullptr;
@@ -356,7 +356,7 @@ extern "C" int ismc_autotune(ismc_ctx* ctx, const ismc_instance* inst, uint32_t 
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     const uint32_t threads_c[] = {128, 256, 512};
-    const uint32_t cpw_c[] = {2, 8, 32};
+    const uint32_t cpw_c[] = {8, 32, 128};
     float best = 1e30f;
     ismc_tune best_t = ctx->tune;
     uint32_t best_cpw = ctx->chunks_per_warp;
