@@ -1,0 +1,80 @@
+"""Edge cases of the propagator, bit-exact against the FP32 twin
+(oracle/ismc_twin.c) through the C ABI: the largest stack the ABI holds,
+packet ids above 2^32, a single packet, one-layer slabs with and without
+spheres, non-scattering layers only, and the batch-size limits."""
+import ctypes as C
+
+import pytest
+
+import oracle
+from ismc_gb300 import Layer, Spheres, _abi, make_instance
+from ismc_gb300.workloads import bench_spheres
+
+pytestmark = pytest.mark.gpu
+
+
+def _same(a, b):
+    return (list(a.sum) == list(b.sum) and list(a.sumsq) == list(b.sumsq) and a.steps == b.steps
+            and a.events == b.events and a.reincidences == b.reincidences and a.capped == b.capped
+            and a.trapped == b.trapped and a.n == b.n)
+
+
+def _check(engine, inst):
+    g = engine.run_batch_raw([inst])[0]
+    t = oracle.twin_run(inst)
+    assert g.status == 0
+    assert _same(g, t), (list(g.sum), list(t.sum), g.steps, t.steps)
+    return g
+
+
+@pytest.mark.parametrize("mode", ["compat", "physical"])
+def test_sixteen_layer_stack(engine, mode):
+    """ISMC_MAXL = 16 layers: two slides around 14 tissue layers."""
+    tissue = [Layer(1.33 + 0.01 * k, 0.1 + 0.2 * k, 20.0 + 7.0 * k, 0.6 + 0.02 * k, 0.01 + 0.003 * k)
+              for k in range(14)]
+    layers = [Layer.slide(1.52, 0.1)] + tissue + [Layer.slide(1.5, 0.12)]
+    assert len(layers) == 16
+    g = _check(engine, make_instance(layers, bench_spheres(), 20000, seed=5, mode=mode))
+    assert g.steps > 0
+
+
+def test_packet_ids_above_2_pow_32(engine):
+    """Packet ids feed two counter words of Philox: ranges crossing 2^32 and far
+    above it are drawn exactly as the twin draws them."""
+    layers = [Layer.slide(1.5, 0.1), Layer(1.4, 1.0, 100.0, 0.9, 0.1), Layer.slide(1.5, 0.1)]
+    for off in ((1 << 32) - 7000, (1 << 40) + 12345):
+        _check(engine, make_instance(layers, bench_spheres(), 15000, seed=8, packet_offset=off))
+
+
+def test_single_packet_and_single_slab(engine):
+    slab = [Layer(1.4, 0.5, 50.0, 0.8, 0.2)]
+    _check(engine, make_instance(slab, bench_spheres(), 1, seed=3))
+    no_spheres = Spheres(R=False, T=False)
+    _check(engine, make_instance(slab, no_spheres, 30000, seed=4))
+    r_only = Spheres(R=True, T=False)
+    _check(engine, make_instance(slab, r_only, 30000, seed=4, roulette_threshold=1e-3))
+
+
+def test_non_scattering_stack(engine):
+    """Only slides: no photon steps; every packet ends as specular, unscattered
+    transmission or absorption in the glass (physical mode)."""
+    glass = [Layer(1.5, 0.0, 0.0, 0.0, 0.1), Layer(1.45, 0.0, 0.0, 0.0, 0.2)]
+    g = _check(engine, make_instance(glass, bench_spheres(), 20000, seed=6))
+    assert g.steps == 0
+    _check(engine, make_instance([Layer(1.5, 0.7, 0.0, 0.0, 0.3)], bench_spheres(), 20000, seed=6,
+                                 mode="physical"))
+
+
+def test_batch_size_limits(engine):
+    """An empty batch is an argument error; a batch of many one-packet
+    instances runs each exactly once."""
+    lib = engine.lib
+    out = _abi.Tally()
+    rc = lib.ismc_run_batch(engine.h, None, 0, None, C.byref(out))
+    assert rc == -1
+    layers = [Layer(1.4, 1.0, 30.0, 0.7, 0.05)]
+    insts = [make_instance(layers, bench_spheres(), 1, seed=11, stream=k) for k in range(5000)]
+    res = engine.run_batch_raw(insts)
+    assert all(t.n == 1 and t.status == 0 for t in res)
+    for k in (0, 1, 2499, 4999):
+        assert _same(res[k], oracle.twin_run(insts[k]))
