@@ -4,7 +4,7 @@
 #include <stdint.h>
 #include "../../include/ismc.h"
 
-#define ISMC_HDR_WORDS 20
+#define ISMC_HDR_WORDS 40
 #define ISMC_LAYER_FIELDS 14
 
 // Layer flags
@@ -30,6 +30,10 @@ struct DevInst {
     float roul_thr, roul_m, roul_inv_m;
     float eta_in[2];            // 1/n of the top / bottom layer (ambient -> sample)
     uint32_t _hpad[2];
+    // Philox key schedule of the instance's seed: round r uses
+    // (rk[2r], rk[2r+1]) = (seed_lo + r W0, seed_hi + r W1) mod 2^32, read as
+    // five 16-byte words (byte offset 80, 16-byte aligned)
+    uint32_t rk[20];
     // per layer, MAXL each
     float n[ISMC_MAXL];
     float mut[ISMC_MAXL];

@@ -13,6 +13,7 @@
 // The reference GPU kernel this replaces is CUDA/CUDAISMLMC.h:132-654.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stddef.h>
 #include "ismc_dev.h"
 #include "ismc_math.cuh"
 
@@ -134,6 +135,10 @@ __global__ void ismc_prepare_kernel(const ismc_instance* __restrict__ in, uint32
     D.stream = I.stream;
     D.seed_lo = (uint32_t)(I.seed & 0xFFFFFFFFull);
     D.seed_hi = (uint32_t)(I.seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        D.rk[2 * r] = D.seed_lo + (uint32_t)r * ISMC_PHILOX_W0;
+        D.rk[2 * r + 1] = D.seed_hi + (uint32_t)r * ISMC_PHILOX_W1;
+    }
     D.cos_port[0] = (float)cR;
     D.cos_port[1] = (float)cT;
     D.p_reinc[0] = (float)pR;
@@ -321,6 +326,9 @@ struct WarpSlots {
     DevInst slot[2];
     unsigned long long acc[2][ISMC_NACC];
 };
+// the round keys are read as 16-byte words from every slot of every warp
+static_assert(offsetof(DevInst, rk) % 16 == 0, "DevInst::rk alignment");
+static_assert(sizeof(DevInst) % 16 == 0 && sizeof(WarpSlots) % 16 == 0, "slot alignment");
 
 #define PH_INCIDENT 0u
 #define PH_WALK 1u
@@ -461,7 +469,8 @@ ismc_propagate_kernel(const PropParams P) {
         const DevInst& I = ws->slot[slot];
         const uint32_t L = I.L;
         const bool compat = I.mode == ISMC_MODE_COMPAT;
-        const ismc_u4 r = ismc_philox4x32_10(ev, pk_lo, pk_hi, I.stream, I.seed_lo, I.seed_hi);
+        const ismc_u4 r = ismc_philox4x32_10_rk(ev, pk_lo, pk_hi, I.stream,
+                                                reinterpret_cast<const uint4*>(I.rk));
         ++ev;
         const float u0 = ismc_u01(r.x);
         int fin = 0;          // 1: packet ended, 2: event cap, 3: trapped in a slide

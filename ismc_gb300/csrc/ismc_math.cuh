@@ -36,6 +36,26 @@ __device__ __forceinline__ ismc_u4 ismc_philox4x32_10(uint32_t c0, uint32_t c1, 
     return ismc_u4{c0, c1, c2, c3};
 }
 
+// The same generator with the key schedule precomputed: rk4[q] holds the keys
+// of rounds 2q and 2q+1 as (k0, k1, k0', k1'), so the per-round key additions
+// become one 16-byte shared-memory load per two rounds.
+__device__ __forceinline__ ismc_u4 ismc_philox4x32_10_rk(uint32_t c0, uint32_t c1, uint32_t c2,
+                                                         uint32_t c3, const uint4* rk4) {
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        const uint4 kk = rk4[q];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t k0 = h ? kk.z : kk.x, k1 = h ? kk.w : kk.y;
+            const uint32_t lo0 = ISMC_PHILOX_M0 * c0, hi0 = __umulhi(ISMC_PHILOX_M0, c0);
+            const uint32_t lo1 = ISMC_PHILOX_M1 * c2, hi1 = __umulhi(ISMC_PHILOX_M1, c2);
+            const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+            c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        }
+    }
+    return ismc_u4{c0, c1, c2, c3};
+}
+
 // Uniform in the open interval (0,1) with 23-bit resolution: (k + 1/2) * 2^-23,
 // k = top 23 bits.  Built as [1,2) mantissa fill minus (1 - 2^-24), which is
 // exact.  Never returns 0 or 1, so "u < p" has probability p for every p in
