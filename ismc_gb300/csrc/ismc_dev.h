@@ -5,7 +5,7 @@
 #include "../../include/ismc.h"
 
 #define ISMC_HDR_WORDS 40
-#define ISMC_LAYER_FIELDS 14
+#define ISMC_LAYER_FIELDS 16
 
 // Layer flags
 #define ISMC_LF_GLASS 1u   // mus == 0: no scattering (ISMLMC.py:81, MLMC.py:97)
@@ -15,12 +15,24 @@
 #define ISMC_IF_RSPHERE 1u
 #define ISMC_IF_TSPHERE 2u
 
+// Per-layer constants, grouped so that each event reads them as 16-byte
+// shared-memory words: q0 what an interaction needs, q1 the Henyey-Greenstein
+// constants, q2 the geometry and interface index ratios, q3 the rest.
+struct DevLayer {
+    float mut, inv_mut, drop, hgc;          // q0; drop: tissue mua/mut per interaction, glass mua (1/cm)
+    float hgd, hge, hga, hgb;               // q1: 1-g, 2g, 1/(2g), 1+g^2 (hgc = 1-g^2)
+    float z_top, z_bot, eta_up, eta_dn;     // q2: eta_up = n/n(above), eta_dn = n/n(below)
+    float n;                                // q3
+    uint32_t lflags;
+    uint32_t _pad[2];
+};
+static_assert(sizeof(DevLayer) == 64, "DevLayer layout");
+
 // Prepared instance: everything the walk needs, derived once per launch by
-// ismc_prepare_kernel.  Stored structure-of-arrays so that lanes reading the
-// same field of different layers hit distinct shared-memory banks.  One warp
-// copies it word by word into its shared-memory slot.
+// ismc_prepare_kernel: a 40-word header, then one DevLayer per layer.  One
+// warp copies it word by word into its shared-memory slot.
 struct DevInst {
-    // header: 20 words
+    // header: 40 words
     uint32_t L, mode, flags, stream;
     uint32_t seed_lo, seed_hi;
     float t_tot;                // total thickness (bottom of the stack)
@@ -29,26 +41,13 @@ struct DevInst {
     float ux0, uz0;             // launch direction
     float roul_thr, roul_m, roul_inv_m;
     float eta_in[2];            // 1/n of the top / bottom layer (ambient -> sample)
-    uint32_t _hpad[2];
+    uint32_t stream_k1;         // stream ^ rk[1]: the constant half of Philox round 0
+    uint32_t _hpad;
     // Philox key schedule of the instance's seed: round r uses
     // (rk[2r], rk[2r+1]) = (seed_lo + r W0, seed_hi + r W1) mod 2^32, read as
     // five 16-byte words (byte offset 80, 16-byte aligned)
     uint32_t rk[20];
-    // per layer, MAXL each
-    float n[ISMC_MAXL];
-    float mut[ISMC_MAXL];
-    float inv_mut[ISMC_MAXL];
-    float drop[ISMC_MAXL];      // tissue: mua/mut per interaction; glass: mua (1/cm)
-    float hga[ISMC_MAXL];       // Henyey-Greenstein constants: 1/(2g)
-    float hgb[ISMC_MAXL];       //   1 + g^2
-    float hgc[ISMC_MAXL];       //   1 - g^2
-    float hgd[ISMC_MAXL];       //   1 - g
-    float hge[ISMC_MAXL];       //   2 g
-    float z_top[ISMC_MAXL];
-    float z_bot[ISMC_MAXL];
-    float eta_up[ISMC_MAXL];    // n[l] / n(above)   (ambient 1 above layer 0)
-    float eta_dn[ISMC_MAXL];    // n[l] / n(below)   (ambient 1 below layer L-1)
-    uint32_t lflags[ISMC_MAXL];
+    DevLayer ly[ISMC_MAXL];     // per-layer constants, 64 B each
 };
 
 static_assert(sizeof(DevInst) == 4 * (ISMC_HDR_WORDS + ISMC_LAYER_FIELDS * ISMC_MAXL),

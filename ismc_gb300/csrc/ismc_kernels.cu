@@ -139,6 +139,7 @@ __global__ void ismc_prepare_kernel(const ismc_instance* __restrict__ in, uint32
         D.rk[2 * r] = D.seed_lo + (uint32_t)r * ISMC_PHILOX_W0;
         D.rk[2 * r + 1] = D.seed_hi + (uint32_t)r * ISMC_PHILOX_W1;
     }
+    D.stream_k1 = D.stream ^ D.rk[1];
     D.cos_port[0] = (float)cR;
     D.cos_port[1] = (float)cT;
     D.p_reinc[0] = (float)pR;
@@ -153,7 +154,7 @@ __global__ void ismc_prepare_kernel(const ismc_instance* __restrict__ in, uint32
     D.roul_thr = I.roulette_threshold;
     D.roul_m = I.roulette_m;
     D.roul_inv_m = ok ? __fdiv_rn(1.0f, I.roulette_m) : 0.0f;
-    D._hpad[0] = D._hpad[1] = 0u;
+    D._hpad = 0u;
     // ---------------------------------------------------------------- layers
     float z = 0.0f;
     for (uint32_t l = 0; l < ISMC_MAXL; ++l) {
@@ -162,24 +163,24 @@ __global__ void ismc_prepare_kernel(const ismc_instance* __restrict__ in, uint32
         const float mut = act ? S.mut[l] : 0.0f;
         const float g = act ? S.g[l] : 0.0f;
         const bool glass = act && S.mus[l] == 0.0f;
-        D.n[l] = n;
-        D.mut[l] = mut;
-        D.inv_mut[l] = mut > 0.0f ? __fdiv_rn(1.0f, mut) : 0.0f;
-        D.drop[l] = !act ? 0.0f : (glass ? S.mua[l] : __fdiv_rn(S.mua[l], mut));
+        D.ly[l].n = n;
+        D.ly[l].mut = mut;
+        D.ly[l].inv_mut = mut > 0.0f ? __fdiv_rn(1.0f, mut) : 0.0f;
+        D.ly[l].drop = !act ? 0.0f : (glass ? S.mua[l] : __fdiv_rn(S.mua[l], mut));
         const float g2 = 2.0f * g;
-        D.hga[l] = g != 0.0f ? __fdiv_rn(1.0f, g2) : 0.0f;
-        D.hgb[l] = 1.0f + g * g;
-        D.hgc[l] = 1.0f - g * g;
-        D.hgd[l] = 1.0f - g;
-        D.hge[l] = g2;
-        D.z_top[l] = z;
+        D.ly[l].hga = g != 0.0f ? __fdiv_rn(1.0f, g2) : 0.0f;
+        D.ly[l].hgb = 1.0f + g * g;
+        D.ly[l].hgc = 1.0f - g * g;
+        D.ly[l].hgd = 1.0f - g;
+        D.ly[l].hge = g2;
+        D.ly[l].z_top = z;
         if (act) z = z + S.d[l];
-        D.z_bot[l] = z;
+        D.ly[l].z_bot = z;
         const float n_above = (l == 0 || !act) ? 1.0f : S.n[l - 1];
         const float n_below = (l + 1 >= L || !act) ? 1.0f : S.n[l + 1];
-        D.eta_up[l] = __fdiv_rn(n, n_above);
-        D.eta_dn[l] = __fdiv_rn(n, n_below);
-        D.lflags[l] = (glass ? ISMC_LF_GLASS : 0u) | (g == 0.0f ? ISMC_LF_ISO : 0u);
+        D.ly[l].eta_up = __fdiv_rn(n, n_above);
+        D.ly[l].eta_dn = __fdiv_rn(n, n_below);
+        D.ly[l].lflags = (glass ? ISMC_LF_GLASS : 0u) | (g == 0.0f ? ISMC_LF_ISO : 0u);
     }
     D.t_tot = z;
     D.eta_in[0] = __fdiv_rn(1.0f, S.n[0 < L ? 0 : 0]);
@@ -359,8 +360,13 @@ __device__ __forceinline__ void ismc_load_slot(WarpSlots* ws, int s, const DevIn
 __device__ __forceinline__ bool ismc_trapped(const DevInst& I, int l, float uz) {
     const float ci = fabsf(uz);
     const float s = 1.0f - ci * ci;
-    const float eu = I.eta_up[l], ed = I.eta_dn[l];
+    const float eu = I.ly[l].eta_up, ed = I.ly[l].eta_dn;
     return (eu * eu) * s >= 1.0f && (ed * ed) * s >= 1.0f;
+}
+
+// 16-byte word k of layer l's constants (see DevLayer)
+__device__ __forceinline__ float4 ismc_lq(const DevInst& I, int l, int k) {
+    return reinterpret_cast<const float4*>(&I.ly[l])[k];
 }
 
 extern "C" __global__ void __launch_bounds__(ISMC_MAX_THREADS)
@@ -385,91 +391,95 @@ ismc_propagate_kernel(const PropParams P) {
     bool alive = false;
     int slot = 0, layer = 0;
     uint32_t phase = PH_INCIDENT, side = 0;     // side 0 = R (top), 1 = T (bottom)
-    uint32_t ev = 0, pk_lo = 0, pk_hi = 0, steps = 0, reinc = 0;
+    uint32_t ev = 0, steps = 0, reinc = 0;
+    uint32_t pa0 = 0, pa1 = 0;            // the packet id's share of Philox round 0
     float w = 0.f, z = 0.f, ux = 0.f, uy = 0.f, uz = 1.f, tau = 0.f, absorbed = 0.f;
 
     for (;;) {
         // ================================================= hand out packets
         unsigned need = __ballot_sync(ISMC_FULL, !alive);
-        while (need) {
-            if (c_next < c_end) {
-                const unsigned long long avail = c_end - c_next;
-                const unsigned k = (unsigned)min((unsigned long long)__popc(need), avail);
-                const unsigned rank = __popc(need & lt_mask);
-                if (!alive && rank < k) {
-                    const unsigned long long id = c_next + rank;
-                    const DevInst& I = ws->slot[cur];
-                    alive = true;
-                    slot = cur;
-                    pk_lo = (uint32_t)id;
-                    pk_hi = (uint32_t)(id >> 32);
-                    ev = 0; steps = 0; reinc = 0;
-                    phase = PH_INCIDENT; side = 0;
-                    w = 1.0f; absorbed = 0.0f; z = 0.0f; tau = 0.0f; layer = 0;
-                    ux = I.ux0; uy = 0.0f; uz = I.uz0;
-                }
-                c_next += k;
-                need = __ballot_sync(ISMC_FULL, !alive);
-                continue;
-            }
-            if (pend < 0) {
-                if (qdone) break;
-                unsigned long long c = 0;
-                if (lane == 0) c = atomicAdd(P.ctrl, 1ull);
-                c = __shfl_sync(ISMC_FULL, c, 0);
-                if (c >= n_chunks) { qdone = true; break; }
-                // instance owning chunk c: last i with prefix[i] <= c
-                int inst = 0;
-                unsigned long long st = 0, en = 0;
-                if (lane == 0) {
-                    uint32_t lo = 0, hi = P.n_inst;           // prefix[lo] <= c < prefix[hi]
-                    while (hi - lo > 1) {
-                        const uint32_t mid = (lo + hi) >> 1;
-                        if (P.chunk_prefix[mid] <= c) lo = mid; else hi = mid;
+        if (need) {     // every lane busy (the common case): nothing to hand out
+            while (need) {
+                if (c_next < c_end) {
+                    const unsigned long long avail = c_end - c_next;
+                    const unsigned k = (unsigned)min((unsigned long long)__popc(need), avail);
+                    const unsigned rank = __popc(need & lt_mask);
+                    if (!alive && rank < k) {
+                        const unsigned long long id = c_next + rank;
+                        const DevInst& I = ws->slot[cur];
+                        alive = true;
+                        slot = cur;
+                        const uint32_t id_hi = (uint32_t)(id >> 32);
+                        pa0 = __umulhi(ISMC_PHILOX_M1, id_hi) ^ (uint32_t)id ^ I.rk[0];
+                        pa1 = ISMC_PHILOX_M1 * id_hi;
+                        ev = 0; steps = 0; reinc = 0;
+                        phase = PH_INCIDENT; side = 0;
+                        w = 1.0f; absorbed = 0.0f; z = 0.0f; tau = 0.0f; layer = 0;
+                        ux = I.ux0; uy = 0.0f; uz = I.uz0;
                     }
-                    inst = (int)lo;
-                    const DevRange R = P.range[lo];
-                    const unsigned long long chunk_packets = P.ctrl[1];
-                    const unsigned long long j = c - P.chunk_prefix[lo];
-                    st = R.offset + j * chunk_packets;
-                    en = R.offset + min((unsigned long long)R.count, (j + 1) * chunk_packets);
+                    c_next += k;
+                    need = __ballot_sync(ISMC_FULL, !alive);
+                    continue;
                 }
-                pend = __shfl_sync(ISMC_FULL, inst, 0);
-                p_next = __shfl_sync(ISMC_FULL, st, 0);
-                p_end = __shfl_sync(ISMC_FULL, en, 0);
+                if (pend < 0) {
+                    if (qdone) break;
+                    unsigned long long c = 0;
+                    if (lane == 0) c = atomicAdd(P.ctrl, 1ull);
+                    c = __shfl_sync(ISMC_FULL, c, 0);
+                    if (c >= n_chunks) { qdone = true; break; }
+                    // instance owning chunk c: last i with prefix[i] <= c
+                    int inst = 0;
+                    unsigned long long st = 0, en = 0;
+                    if (lane == 0) {
+                        uint32_t lo = 0, hi = P.n_inst;           // prefix[lo] <= c < prefix[hi]
+                        while (hi - lo > 1) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (P.chunk_prefix[mid] <= c) lo = mid; else hi = mid;
+                        }
+                        inst = (int)lo;
+                        const DevRange R = P.range[lo];
+                        const unsigned long long chunk_packets = P.ctrl[1];
+                        const unsigned long long j = c - P.chunk_prefix[lo];
+                        st = R.offset + j * chunk_packets;
+                        en = R.offset + min((unsigned long long)R.count, (j + 1) * chunk_packets);
+                    }
+                    pend = __shfl_sync(ISMC_FULL, inst, 0);
+                    p_next = __shfl_sync(ISMC_FULL, st, 0);
+                    p_end = __shfl_sync(ISMC_FULL, en, 0);
+                }
+                // place the pending chunk into a slot
+                const int cur_inst = cur ? s_inst1 : s_inst0;
+                const int oth_inst = cur ? s_inst0 : s_inst1;
+                if (pend == cur_inst) {
+                    c_next = p_next; c_end = p_end; pend = -1;
+                    continue;
+                }
+                if (pend == oth_inst) {
+                    cur ^= 1; c_next = p_next; c_end = p_end; pend = -1;
+                    continue;
+                }
+                const bool oth_busy = __any_sync(ISMC_FULL, alive && slot == (cur ^ 1));
+                const bool cur_busy = __any_sync(ISMC_FULL, alive && slot == cur);
+                int tgt = -1;
+                if (!oth_busy) tgt = cur ^ 1; else if (!cur_busy) tgt = cur;
+                if (tgt < 0) break;                    // both slots still draining: wait
+                ismc_flush_slot(ws, tgt, tgt ? s_inst1 : s_inst0, P.tally, lane);
+                ismc_load_slot(ws, tgt, P.inst + pend, lane);
+                if (tgt) s_inst1 = pend; else s_inst0 = pend;
+                cur = tgt; c_next = p_next; c_end = p_end; pend = -1;
             }
-            // place the pending chunk into a slot
-            const int cur_inst = cur ? s_inst1 : s_inst0;
-            const int oth_inst = cur ? s_inst0 : s_inst1;
-            if (pend == cur_inst) {
-                c_next = p_next; c_end = p_end; pend = -1;
+            if (!__any_sync(ISMC_FULL, alive)) {
+                if (qdone && pend < 0) break;
                 continue;
             }
-            if (pend == oth_inst) {
-                cur ^= 1; c_next = p_next; c_end = p_end; pend = -1;
-                continue;
-            }
-            const bool oth_busy = __any_sync(ISMC_FULL, alive && slot == (cur ^ 1));
-            const bool cur_busy = __any_sync(ISMC_FULL, alive && slot == cur);
-            int tgt = -1;
-            if (!oth_busy) tgt = cur ^ 1; else if (!cur_busy) tgt = cur;
-            if (tgt < 0) break;                    // both slots still draining: wait
-            ismc_flush_slot(ws, tgt, tgt ? s_inst1 : s_inst0, P.tally, lane);
-            ismc_load_slot(ws, tgt, P.inst + pend, lane);
-            if (tgt) s_inst1 = pend; else s_inst0 = pend;
-            cur = tgt; c_next = p_next; c_end = p_end; pend = -1;
+            if (!alive) continue;
         }
-        if (!__any_sync(ISMC_FULL, alive)) {
-            if (qdone && pend < 0) break;
-            continue;
-        }
-        if (!alive) continue;
 
         // ================================================= one event
         const DevInst& I = ws->slot[slot];
         const uint32_t L = I.L;
         const bool compat = I.mode == ISMC_MODE_COMPAT;
-        const ismc_u4 r = ismc_philox4x32_10_rk(ev, pk_lo, pk_hi, I.stream,
+        const ismc_u4 r = ismc_philox4x32_10_ev(ev, pa0, pa1, I.stream_k1,
                                                 reinterpret_cast<const uint4*>(I.rk));
         ++ev;
         const float u0 = ismc_u01(r.x);
@@ -488,11 +498,12 @@ ismc_propagate_kernel(const PropParams P) {
             const float eta = I.eta_in[top ? 0 : 1];
             float ct;
             float R = ismc_fresnel(eta, c, &ct);
-            if (compat && (I.lflags[l] & ISMC_LF_GLASS)) {
+            const bool lglass = (I.ly[l].lflags & ISMC_LF_GLASS) != 0u;
+            if (compat && lglass) {
                 // slide on the incidence face: two-interface series with the
                 // ambient-side cosine for both interfaces (ISMLMC.py:81-91)
                 float ct2;
-                const float r2 = ismc_fresnel(top ? I.eta_dn[l] : I.eta_up[l], c, &ct2);
+                const float r2 = ismc_fresnel(top ? I.ly[l].eta_dn : I.ly[l].eta_up, c, &ct2);
                 const float om = 1.0f - R;
                 R = R + __fdiv_rn((om * om) * r2, 1.0f - R * r2);
             }
@@ -506,19 +517,21 @@ ismc_propagate_kernel(const PropParams P) {
                 z = top ? 0.0f : I.t_tot;
                 layer = l;
                 phase = PH_WALK;
-                tau = (compat && (I.lflags[l] & ISMC_LF_GLASS)) ? 0.0f : ismc_neglog_u32(r.w);
-                if ((I.lflags[l] & ISMC_LF_GLASS) && ismc_trapped(I, l, uz)) fin = 3;
+                tau = (compat && lglass) ? 0.0f : ismc_neglog_u32(r.w);
+                if (lglass && ismc_trapped(I, l, uz)) fin = 3;
             }
         } else {
             // -------- walk inside layer l (MLMC.py:95-200)
             const int l = layer;
             const bool down = uz > 0.0f;
-            const bool glass = (I.lflags[l] & ISMC_LF_GLASS) != 0u;
-            const float zb = down ? I.z_bot[l] : I.z_top[l];
+            const bool glass = (I.ly[l].lflags & ISMC_LF_GLASS) != 0u;
+            const float4 q0 = ismc_lq(I, l, 0);     // mut, inv_mut, drop, hgc
+            const float4 q2 = ismc_lq(I, l, 2);     // z_top, z_bot, eta_up, eta_dn
+            const float zb = down ? q2.y : q2.x;
             // distance to the boundary along z (rounding can leave z a hair outside)
             const float dist = fmaxf(down ? zb - z : z - zb, 0.0f);
             const float auz = fabsf(uz);
-            const float mut = I.mut[l];
+            const float mut = q0.x;
             if (glass && auz == 0.0f) {
                 fin = 2;                                   // cannot leave a slide: give up on it
             } else if (glass || (auz > 0.0f && dist * mut <= tau * auz)) {
@@ -526,15 +539,15 @@ ismc_propagate_kernel(const PropParams P) {
                 if (!glass) {
                     const float d = __fdiv_rn(dist, auz);
                     tau = fmaxf(__fmaf_rn(-d, mut, tau), 0.0f);
-                } else if (!compat && I.drop[l] > 0.0f) {
+                } else if (!compat && q0.z > 0.0f) {
                     const float d = __fdiv_rn(dist, auz);
-                    const float wn = w * ismc_expneg(I.drop[l] * d);
+                    const float wn = w * ismc_expneg(q0.z * d);
                     absorbed = absorbed + (w - wn);
                     w = wn;
                 }
                 z = zb;
                 const int nl = down ? l + 1 : l - 1;
-                const float eta = down ? I.eta_dn[l] : I.eta_up[l];
+                const float eta = down ? q2.w : q2.z;
                 float ct;
                 const float R = ismc_fresnel(eta, auz, &ct);
                 if (u0 < R) {
@@ -549,15 +562,16 @@ ismc_propagate_kernel(const PropParams P) {
                     uz = down ? ct : -ct;
                     // slide -> tissue leaves no path to spend: the packet
                     // interacts at the interface (MLMC.py:111, 148, 165-200)
-                    if (compat && glass && !(I.lflags[nl] & ISMC_LF_GLASS)) tau = 0.0f;
+                    const bool nglass = (I.ly[nl].lflags & ISMC_LF_GLASS) != 0u;
+                    if (compat && glass && !nglass) tau = 0.0f;
                     layer = nl;
-                    if ((I.lflags[nl] & ISMC_LF_GLASS) && ismc_trapped(I, nl, uz)) fin = 3;
+                    if (nglass && ismc_trapped(I, nl, uz)) fin = 3;
                 }
             } else {
                 // ---- interaction inside the layer: hop, drop, roulette, spin
-                const float s = tau * I.inv_mut[l];
+                const float s = tau * q0.y;
                 z = __fmaf_rn(s, uz, z);
-                const float dw = w * I.drop[l];
+                const float dw = w * q0.z;
                 w = w - dw;
                 absorbed = absorbed + dw;
                 ++steps;
@@ -568,11 +582,12 @@ ismc_propagate_kernel(const PropParams P) {
                 if (!fin) {
                     const float u1 = ismc_u01(r.y), u2 = ismc_u01(r.z);
                     float cth;
-                    if (I.lflags[l] & ISMC_LF_ISO) {
+                    if (I.ly[l].lflags & ISMC_LF_ISO) {
                         cth = 2.0f * u1 - 1.0f;
                     } else {
-                        const float t = __fdiv_rn(I.hgc[l], __fmaf_rn(I.hge[l], u1, I.hgd[l]));
-                        cth = I.hga[l] * __fmaf_rn(-t, t, I.hgb[l]);
+                        const float4 q1 = ismc_lq(I, l, 1);     // hgd, hge, hga, hgb
+                        const float t = __fdiv_rn(q0.w, __fmaf_rn(q1.y, u1, q1.x));
+                        cth = q1.z * __fmaf_rn(-t, t, q1.w);
                         cth = fminf(fmaxf(cth, -1.0f), 1.0f);
                     }
                     float sp, cp;

@@ -56,6 +56,26 @@ __device__ __forceinline__ ismc_u4 ismc_philox4x32_10_rk(uint32_t c0, uint32_t c
     return ismc_u4{c0, c1, c2, c3};
 }
 
+// The same block with the parts of round 0 that do not depend on the event
+// index folded in ahead of time, for counters (ev, pk_lo, pk_hi, stream):
+//   a0 = umulhi(M1, pk_hi) ^ pk_lo ^ k0,  a1 = M1 * pk_hi   (per packet)
+//   b  = stream ^ k1                                          (per instance)
+// Rounds 1-9 take their keys from rk4 as above.
+__device__ __forceinline__ ismc_u4 ismc_philox4x32_10_ev(uint32_t ev, uint32_t a0, uint32_t a1,
+                                                         uint32_t b, const uint4* rk4) {
+    uint32_t c0 = a0, c1 = a1, c2 = __umulhi(ISMC_PHILOX_M0, ev) ^ b, c3 = ISMC_PHILOX_M0 * ev;
+#pragma unroll
+    for (int r = 1; r < 10; ++r) {
+        const uint4 kk = rk4[r >> 1];
+        const uint32_t k0 = (r & 1) ? kk.z : kk.x, k1 = (r & 1) ? kk.w : kk.y;
+        const uint32_t lo0 = ISMC_PHILOX_M0 * c0, hi0 = __umulhi(ISMC_PHILOX_M0, c0);
+        const uint32_t lo1 = ISMC_PHILOX_M1 * c2, hi1 = __umulhi(ISMC_PHILOX_M1, c2);
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    }
+    return ismc_u4{c0, c1, c2, c3};
+}
+
 // Uniform in the open interval (0,1) with 23-bit resolution: (k + 1/2) * 2^-23,
 // k = top 23 bits.  Built as [1,2) mantissa fill minus (1 - 2^-24), which is
 // exact.  Never returns 0 or 1, so "u < p" has probability p for every p in
