@@ -120,7 +120,26 @@ def run_solve(engine, sur, n_meas=10000, n_plain=200, seed=4, verify_packets=1_0
         return {"median": np.median(e, 0).tolist(), "p90": np.percentile(e, 90, 0).tolist(),
                 "within_2pct": np.mean(e <= 0.02, 0).tolist()}
 
+    # noise-free measurements: the two paths then differ only by the plain
+    # objective's Monte Carlo noise and the surrogate's error
+    m0 = min(n_meas, 1000)
+    k0 = min(k, 200)
+    truth0, meas0 = make_measurements(engine, m0, seed=seed + 17, noise=(0.0, 0.0, 0.0))
+    reqs0 = [make_solve(sample_stack(1.0, 10.0, 0.9, 0.1, 1.4), 1, sph, plain_packets,
+                        (meas0[i, 0], None, meas0[i, 1], meas0[i, 2]), x0=(0.3, 10.0),
+                        seed=seed + 5000 + i, lo=SOLVE_LO, hi=SOLVE_HI, max_evals=400)
+             for i in range(k0)]
+    xp0 = np.array([[o.x[0], o.x[1]] for o in engine.solve_batch(reqs0)])
+    r0 = surrogate_solve(sur, engine, meas0, sig, verify_packets=verify_packets,
+                         plain_packets=plain_packets, seed=seed + 199)
+    noise_free = {"measurements": m0, "plain_subsample": k0,
+                  "plain_rel_err_vs_truth": rel(xp0, truth0[:k0]),
+                  "surrogate_rel_err_vs_truth": rel(r0["x"], truth0),
+                  "surrogate_vs_plain_rel_diff": rel(r0["x"][:k0], xp0),
+                  "fallback_rate": float(r0["fallback"].mean())}
+
     return {"measurements": n_meas, "plain_subsample": k, "objective": "chi2",
+            "noise_free": noise_free,
             "plain_solves_per_s": k / t_plain, "plain_evals_mean": float(ev.mean()),
             "plain_rel_err_vs_truth": rel(xp, truth[:k]),
             "surrogate_solves_per_s": n_meas / t_sur,
