@@ -190,7 +190,7 @@ int ismc_run_batch_device(ismc_ctx* ctx, const ismc_instance* d_inst, uint32_t n
  * memory, a fixed memory budget, or a loop that cannot take an allocation's
  * implicit synchronisation.  Inputs and outputs are the caller's device
  * pointers, as for ismc_run_batch_device; the library's working memory is one
- * fixed __device__ array sized for ISMC_NOALLOC_MAX_INST instances (~1 MB,
+ * fixed __device__ array sized for ISMC_NOALLOC_MAX_INST instances (~1.2 MB,
  * kept by every GPU that loads the library until the process exits).
  *   - Needs no context; runs on the calling thread's current device and on
  *     `stream` as given (NULL = legacy default stream).

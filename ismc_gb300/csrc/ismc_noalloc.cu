@@ -11,7 +11,7 @@
 // The working memory that ismc_run_batch_device takes from a context (prepared
 // tables, packet ranges, work-queue prefix, queue head and chunk size) lives
 // here in one file-scope __device__ array of fixed size, sized for at most
-// ISMC_NOALLOC_MAX_INST instances (about 1 MB).  Every GPU that loads the
+// ISMC_NOALLOC_MAX_INST instances (about 1.2 MB).  Every GPU that loads the
 // library keeps that array until the process exits.
 #include <cuda_runtime.h>
 #include <algorithm>
