@@ -345,6 +345,18 @@ __device__ __forceinline__ void ismc_flush_slot(WarpSlots* ws, int s, int inst, 
     __syncwarp();
 }
 
+// A lane's step, event and re-incidence counts run up in registers across its
+// packets and reach the slot's accumulators only when the lane moves to the
+// other slot, when that slot is recycled, before a count could pass 2^31, and
+// when the warp retires (integer sums: the order of additions is irrelevant).
+__device__ __forceinline__ void ismc_flush_counts(unsigned long long* acc, uint32_t& lsteps,
+                                                  uint32_t& lev, uint32_t& lreinc) {
+    if (lsteps) atomicAdd(acc + 10, (unsigned long long)lsteps);
+    if (lev) atomicAdd(acc + 11, (unsigned long long)lev);
+    if (lreinc) atomicAdd(acc + 12, (unsigned long long)lreinc);
+    lsteps = lev = lreinc = 0u;
+}
+
 __device__ __forceinline__ void ismc_load_slot(WarpSlots* ws, int s, const DevInst* src, int lane) {
     const uint32_t* g = reinterpret_cast<const uint32_t*>(src);
     uint32_t* d = reinterpret_cast<uint32_t*>(&ws->slot[s]);
@@ -391,7 +403,9 @@ ismc_propagate_kernel(const PropParams P) {
     bool alive = false;
     int slot = 0, layer = 0;
     uint32_t phase = PH_INCIDENT, side = 0;     // side 0 = R (top), 1 = T (bottom)
-    uint32_t ev = 0, steps = 0, reinc = 0;
+    uint32_t ev = 0;
+    uint32_t lsteps = 0, lev = 0, lreinc = 0;   // counts not yet in a slot accumulator
+    int lslot = 0;                              // the slot they belong to
     uint32_t pa0 = 0, pa1 = 0;            // the packet id's share of Philox round 0
     float w = 0.f, z = 0.f, ux = 0.f, uy = 0.f, uz = 1.f, tau = 0.f, absorbed = 0.f;
 
@@ -412,7 +426,11 @@ ismc_propagate_kernel(const PropParams P) {
                         const uint32_t id_hi = (uint32_t)(id >> 32);
                         pa0 = __umulhi(ISMC_PHILOX_M1, id_hi) ^ (uint32_t)id ^ I.rk[0];
                         pa1 = ISMC_PHILOX_M1 * id_hi;
-                        ev = 0; steps = 0; reinc = 0;
+                        if (lslot != cur) {
+                            ismc_flush_counts(ws->acc[lslot], lsteps, lev, lreinc);
+                            lslot = cur;
+                        }
+                        ev = 0;
                         phase = PH_INCIDENT; side = 0;
                         w = 1.0f; absorbed = 0.0f; z = 0.0f; tau = 0.0f; layer = 0;
                         ux = I.ux0; uy = 0.0f; uz = I.uz0;
@@ -463,6 +481,8 @@ ismc_propagate_kernel(const PropParams P) {
                 int tgt = -1;
                 if (!oth_busy) tgt = cur ^ 1; else if (!cur_busy) tgt = cur;
                 if (tgt < 0) break;                    // both slots still draining: wait
+                if (lslot == tgt) ismc_flush_counts(ws->acc[tgt], lsteps, lev, lreinc);
+                __syncwarp();
                 ismc_flush_slot(ws, tgt, tgt ? s_inst1 : s_inst0, P.tally, lane);
                 ismc_load_slot(ws, tgt, P.inst + pend, lane);
                 if (tgt) s_inst1 = pend; else s_inst0 = pend;
@@ -574,7 +594,7 @@ ismc_propagate_kernel(const PropParams P) {
                 const float dw = w * q0.z;
                 w = w - dw;
                 absorbed = absorbed + dw;
-                ++steps;
+                ++lsteps;
                 if (w <= I.roul_thr) {                     // MLMC.py:177
                     if (u0 < I.roul_inv_m) w = w * I.roul_m;
                     else { w = 0.0f; fin = 1; }
@@ -636,7 +656,7 @@ ismc_propagate_kernel(const PropParams P) {
                 uy = sp * sn;
                 uz = side ? -mz : mz;
                 phase = PH_INCIDENT;
-                ++reinc;
+                ++lreinc;
             } else {
                 bin = side ? ISMC_T_TD : ISMC_T_RD;
                 fin = 1;
@@ -659,12 +679,13 @@ ismc_propagate_kernel(const PropParams P) {
                 atomicAdd(acc + 13, 1ull);
                 atomicMin(&P.tally[slot ? s_inst1 : s_inst0].status, ISMC_ERR_STEP_LIMIT);
             }
-            atomicAdd(acc + 10, (unsigned long long)steps);
-            atomicAdd(acc + 11, (unsigned long long)ev);
-            if (reinc) atomicAdd(acc + 12, (unsigned long long)reinc);
+            lev += ev;
+            if ((lev | lsteps) >= 0x80000000u) ismc_flush_counts(acc, lsteps, lev, lreinc);
             alive = false;
         }
     }
+    __syncwarp();
+    ismc_flush_counts(ws->acc[lslot], lsteps, lev, lreinc);
     __syncwarp();
     ismc_flush_slot(ws, 0, s_inst0, P.tally, lane);
     ismc_flush_slot(ws, 1, s_inst1, P.tally, lane);
