@@ -31,3 +31,25 @@ def test_gpu_solve_batch_recovers_truth(engine):
         assert abs(o.x[1] / s - 1) < 0.05, (a, s, list(o.x), o.evals)
         # one batched launch per round: rounds never exceed evaluations
         assert 0 < o.rounds <= o.evals
+
+
+def test_minimize_distribution_outer_loop(engine):
+    """minimization.py's outer loop (samples of n and sphere parameters, runs
+    per sample) as one batched solve: every sample's answer lies near the
+    truth, and the spread over samples is reported."""
+    import numpy as np
+    from ismc_gb300.lookup import sample_distributions
+    from ismc_gb300.minimize import minimize_distribution
+    sph = bench_spheres()
+    truth = (0.8, 25.0)
+    m = engine.run_batch([make_instance(_stack(*truth), sph, 4_000_000, seed=31)])[0]
+    samples = sample_distributions(1.4, 0.005, sph, {"R_pw": 0.002, "T_pw": 0.002}, 3, seed=2)
+    meas = np.array([[m["R_d"], np.nan, m["T_d"], m["T_u"]]] * len(samples))
+    res = minimize_distribution(_stack(1.0, 20.0), 1, samples, meas, 200_000, runs=2,
+                                x0=(1.0, 20.0), lo=(0.05, 2.0), hi=(10.0, 200.0), seed=3,
+                                max_evals=300, engine=engine)
+    assert len(res["solves"]) == 6 and all(o.status == 0 for o in res["solves"])
+    assert np.all(np.abs(res["mu_a_per_sample"] / truth[0] - 1) < 0.25), res["mu_a_per_sample"]
+    assert np.all(np.abs(res["mu_s_per_sample"] / truth[1] - 1) < 0.10), res["mu_s_per_sample"]
+    assert abs(res["mu_s"] / truth[1] - 1) < 0.06
+    assert res["mu_a_unc"] >= 0 and res["mu_s_unc"] >= 0
