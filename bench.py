@@ -132,6 +132,53 @@ def cpu_baseline(seconds=12.0):
                       f"{threads} threads, {dt:.1f} s)", "steps_per_s": steps / dt}
 
 
+def cpu_solve_baseline(engine, seconds=60.0, packets=100_000):
+    """The reference's Python minimisation path (minimization.py:199-271:
+    scipy Powell on the reference's cost, one N-packet forward run per
+    objective) with the FP64 restatement of ISMLMC.py on all host cores as
+    the forward model, on a few of the solve benchmark's measurements, for
+    about `seconds`.  Reported beside the GPU paths."""
+    import math
+    import numpy as np
+    from scipy.optimize import minimize
+    import oracle
+    from ismc_gb300 import make_instance
+    from ismc_gb300.benchmarks import make_measurements
+    from ismc_gb300.surrogate import sample_stack
+    from ismc_gb300.workloads import bench_spheres
+    threads = os.cpu_count()
+    sph = bench_spheres()
+    truth, meas = make_measurements(engine, 8, seed=4)
+    evals = [0]
+
+    def cost(x, m, k):
+        mua, musr = float(x[0]), float(x[1])
+        if not (mua > 0.0 and musr > 0.0):
+            return 1e3                        # outside the physical range
+        evals[0] += 1
+        inst = make_instance(sample_stack(mua, musr, 0.9, 0.1, 1.4), sph, packets, seed=900 + k,
+                             stream=evals[0], mode="compat")
+        mean, _, _ = oracle.ref64_run(inst, threads=threads)
+        rd, td, tu = mean[1], mean[3], mean[4]
+        return math.sqrt(((rd - m[0]) / m[0]) ** 2 + ((td - m[1]) / m[1]) ** 2 + (tu - m[2]) ** 2)
+
+    t0 = time.perf_counter()
+    done, errs = 0, []
+    for k in range(len(meas)):
+        if done and time.perf_counter() - t0 > seconds:
+            break
+        res = minimize(cost, [0.3, 10.0], args=(meas[k], k), method="Powell", tol=1e-3,
+                       options={"maxfev": 400})
+        errs.append([abs(res.x[0] / truth[k, 0] - 1), abs(res.x[1] / truth[k, 1] - 1)])
+        done += 1
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"{done} solves of the benchmark's measurements, scipy Powell (tol 1e-3, at most "
+                      f"400 evaluations) on the reference's cost with {packets}-packet FP64 C "
+                      f"restatement runs ({threads} threads), {evals[0]} evaluations, {dt:.1f} s",
+            "rel_err_vs_truth_median": np.median(np.array(errs), 0).tolist()}
+
+
 def load_roofline_profile():
     try:
         with open(ROOFLINE_FILE) as fh:
@@ -312,7 +359,9 @@ def run_other_workload(args):
         if args.workload == "solve":
             sr = benchmarks.run_solve(eng, sur, n_meas=max(256, int(10000 * s)),
                                       n_plain=max(32, int(200 * min(1.0, 4 * s))))
+            cpu = None if args.no_cpu_baseline else cpu_solve_baseline(eng)
             line = {"metric": "inverse solves/s", "value": sr["surrogate_solves_per_s"],
+                    "cpu_baseline": cpu,
                     "unit": "solves/s", "workload": "solve",
                     "config": {"scale": s, "epochs": args.epochs},
                     "result": sr, "surrogate": r}
