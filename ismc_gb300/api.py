@@ -222,6 +222,66 @@ def tally_to_result(t: _abi.Tally) -> Result:
                   sums=[int(x) for x in t.sum], sumsqs=[int(x) for x in t.sumsq])
 
 
+def tallies_mean_se(tallies):
+    """Vectorised tally_to_result for a ctypes array of tallies: (mean [n x 5],
+    se [n x 5], status [n]) with the same FP64 normalisation."""
+    import numpy as np
+    v = np.ctypeslib.as_array(tallies)
+    n = v["n"].astype(np.float64)
+    scale = np.ldexp(1.0, np.where(v["scale_log2"] == 0, 32, v["scale_log2"]).astype(np.int64))
+    s = v["sum"].astype(np.float64) / scale[:, None]
+    q = v["sumsq"].astype(np.float64) / scale[:, None]
+    with np.errstate(invalid="ignore", divide="ignore"):
+        mean = s / n[:, None]
+        ex2 = q / n[:, None]
+        var = np.where(n[:, None] > 1, np.maximum(ex2 - mean * mean, 0.0) * n[:, None] /
+                       np.maximum(n[:, None] - 1, 1), 0.0)
+        se = np.sqrt(var / n[:, None])
+    bad = n == 0
+    mean[bad] = np.nan
+    se[bad] = np.nan
+    return mean, se, v["status"].copy()
+
+
+def slab_instances(mua, mus_reduced, g, d, n, spheres: Spheres, n_packets, seed: int = 0,
+                   stream0: int = 0, mode="compat", slides=((1.5, 0.1), (1.5, 0.1)),
+                   roulette_threshold: float = 1e-4, roulette_m: float = 10.0):
+    """Many one-slab instances between two slides at once: row i is
+    make_instance([Layer.slide(*slides[0]), Layer.from_reduced(n[i], mua[i],
+    mus_reduced[i], g[i], d[i]), Layer.slide(*slides[1])], spheres, n_packets,
+    seed, stream0 + i, mode), filled as a numpy view of the ctypes array."""
+    import numpy as np
+    mua, musr, g, d, n = (np.atleast_1d(np.asarray(x, dtype=np.float64)) for x in
+                          (mua, mus_reduced, g, d, n))
+    m = max(len(mua), len(musr), len(g), len(d), len(n))
+    mua, musr, g, d, n = (np.broadcast_to(x, (m,)) for x in (mua, musr, g, d, n))
+    mus = np.where(g == 1.0, musr, musr / np.where(g == 1.0, 2.0, 1.0 - g))
+    arr = (_abi.Instance * m)()
+    v = np.ctypeslib.as_array(arr)
+    st = v["stack"]
+    st["L"] = 3
+    (n0, d0), (n2, d2) = slides
+    st["n"][:, 0], st["d"][:, 0] = n0, d0
+    st["n"][:, 2], st["d"][:, 2] = n2, d2
+    st["n"][:, 1] = n
+    st["mua"][:, 1] = mua
+    st["mus"][:, 1] = mus
+    st["mut"][:, 1] = mua + mus
+    st["g"][:, 1] = g
+    st["d"][:, 1] = d
+    sp = make_spheres(spheres)
+    for name, _ in _abi.Spheres._fields_:
+        v["spheres"][name] = getattr(sp, name) if not name.startswith("_") else 0
+    v["n_packets"] = int(n_packets)
+    v["packet_offset"] = 0
+    v["seed"] = int(seed) & 0xFFFFFFFFFFFFFFFF
+    v["stream"] = (np.arange(m, dtype=np.uint64) + np.uint64(stream0)) & np.uint64(0xFFFFFFFF)
+    v["mode"] = MODES[mode]
+    v["roulette_threshold"] = roulette_threshold
+    v["roulette_m"] = roulette_m
+    return arr
+
+
 def make_solve(layers: Sequence[Layer], layer: int, spheres: Spheres, n_packets: int,
                meas, x0, lo=(1e-6, 1e-6), hi=(1e6, 1e6), seed: int = 0, separate=False,
                log_coords=True, h0=None, t0=None, max_evals=400, max_restarts=3,

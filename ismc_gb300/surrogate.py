@@ -23,7 +23,8 @@ import time
 import numpy as np
 
 from . import _abi
-from .api import Engine, IsmcError, Layer, load_library, make_instance, make_solve
+from .api import (Engine, IsmcError, Layer, load_library, make_solve, slab_instances,
+                  tallies_mean_se)
 from .workloads import bench_spheres
 
 LO = np.array([math.log(0.01), math.log(1.0), 0.6, 0.02, 1.33])
@@ -43,19 +44,20 @@ def sample_inputs(n, seed=42):
 
 def simulate(engine, X, n_packets, seed=42, chunk=65536, spheres=None, mode="compat"):
     """Monte Carlo targets for input rows X: returns (Y means [n x 3], SE [n x 3])
-    of (R_d, T_d, T_u), one batched launch per chunk of rows."""
+    of (R_d, T_d, T_u), one batched launch per chunk of rows; row i runs
+    sample_stack(exp X[i,0], exp X[i,1], X[i,2], X[i,3], X[i,4]) on Philox
+    stream i."""
     sph = spheres or bench_spheres()
+    X = np.asarray(X, dtype=np.float64)
     Y = np.empty((len(X), 3))
     S = np.empty((len(X), 3))
     for a in range(0, len(X), chunk):
         rows = X[a:a + chunk]
-        insts = [make_instance(sample_stack(math.exp(r[0]), math.exp(r[1]), r[2], r[3], r[4]),
-                               sph, n_packets, seed=seed, stream=a + i, mode=mode)
-                 for i, r in enumerate(rows)]
-        res = engine.run_batch(insts)
-        for i, t in enumerate(res):
-            Y[a + i] = (t.mean[1], t.mean[3], t.mean[4])
-            S[a + i] = (t.se[1], t.se[3], t.se[4])
+        insts = slab_instances(np.exp(rows[:, 0]), np.exp(rows[:, 1]), rows[:, 2], rows[:, 3],
+                               rows[:, 4], sph, n_packets, seed=seed, stream0=a, mode=mode)
+        mean, se, _ = tallies_mean_se(engine.run_batch_raw(insts))
+        Y[a:a + len(rows)] = mean[:, [1, 3, 4]]
+        S[a:a + len(rows)] = se[:, [1, 3, 4]]
     return Y, S
 
 
@@ -217,13 +219,10 @@ def _gauss_newton(sur, x, meas, w, offset, steps, g, d, n, h=0.05):
 
 
 def _verify(engine, x, g, d, n, packets, seed, stream0=0):
-    sph = bench_spheres()
-    insts = [make_instance(sample_stack(math.exp(x[i, 0]), math.exp(x[i, 1]), g, d, n), sph,
-                           packets, seed=seed, stream=stream0 + i) for i in range(len(x))]
-    res = engine.run_batch(insts)
-    V = np.array([[r.mean[1], r.mean[3], r.mean[4]] for r in res])
-    VS = np.array([[r.se[1], r.se[3], r.se[4]] for r in res])
-    return V, VS
+    insts = slab_instances(np.exp(x[:, 0]), np.exp(x[:, 1]), g, d, n, bench_spheres(), packets,
+                           seed=seed, stream0=stream0)
+    mean, se, _ = tallies_mean_se(engine.run_batch_raw(insts))
+    return mean[:, [1, 3, 4]], se[:, [1, 3, 4]]
 
 
 def objective_weights(meas, sigma, objective="chi2"):

@@ -1,0 +1,46 @@
+"""Host-side helpers that need no GPU: the vectorised instance builder and
+tally normalisation agree with their one-at-a-time counterparts."""
+import math
+
+import numpy as np
+
+from ismc_gb300 import _abi, api
+from ismc_gb300.surrogate import sample_stack
+from ismc_gb300.workloads import bench_spheres
+
+
+def test_slab_instances_are_byte_identical_to_make_instance():
+    rng = np.random.default_rng(0)
+    X = np.stack([rng.uniform(-4.6, 2.3, 64), rng.uniform(0, 4.6, 64), rng.uniform(0.6, 1.0, 64),
+                  rng.uniform(0.02, 0.5, 64), rng.uniform(1.33, 1.5, 64)], 1)
+    X[3, 2] = 1.0                                 # g = 1: mu_s = mu_s'
+    sph = bench_spheres()
+    for mode in ("compat", "physical"):
+        arr = api.slab_instances(np.exp(X[:, 0]), np.exp(X[:, 1]), X[:, 2], X[:, 3], X[:, 4], sph,
+                                 54321, seed=(1 << 40) + 7, stream0=1000, mode=mode)
+        for i, r in enumerate(X):
+            ref = api.make_instance(sample_stack(math.exp(r[0]), math.exp(r[1]), r[2], r[3], r[4]),
+                                    sph, 54321, seed=(1 << 40) + 7, stream=1000 + i, mode=mode)
+            assert bytes(arr[i]) == bytes(ref), i
+
+
+def test_tallies_mean_se_matches_tally_to_result():
+    rng = np.random.default_rng(1)
+    out = (_abi.Tally * 6)()
+    for i, t in enumerate(out):
+        t.n = [0, 1, 2, 1000, 123457, 10 ** 8][i]
+        t.scale_log2 = 32
+        for k in range(5):
+            m = float(rng.random())
+            t.sum[k] = int(m * t.n * 2 ** 32)
+            t.sumsq[k] = int(m * m * 1.3 * t.n * 2 ** 32)
+        t.status = -3 if i == 2 else 0
+    mean, se, status = api.tallies_mean_se(out)
+    for i, t in enumerate(out):
+        r = api.tally_to_result(t)
+        assert status[i] == r.status
+        for k in range(5):
+            if math.isnan(r.mean[k]):
+                assert np.isnan(mean[i, k]) and np.isnan(se[i, k])
+            else:
+                assert mean[i, k] == r.mean[k] and se[i, k] == r.se[k], (i, k)
