@@ -236,7 +236,9 @@ typedef struct ismc_solve_req {
                                  evaluation, like the reference's global random state */
     double meas[4];           /* measured R_d, R_s, T_d, T_u; NaN = not measured */
     double x0[2];             /* initial (mu_a, mu_s') */
-    double lo[2], hi[2];      /* accepted box for (mu_a, mu_s') */
+    double lo[2], hi[2];      /* accepted box for (mu_a, mu_s'): answers outside it are
+                                 re-run (max_restarts); the objective is evaluated only
+                                 inside it, widened to take in an x0 that lies outside */
     double h0, t0;            /* PRAXIS initial step and tolerance (in the chosen coordinates) */
 } ismc_solve_req;
 

@@ -62,8 +62,15 @@ int build_request(Solve& s, uint32_t index, const double* p, std::vector<ismc_in
     // outside the accepted box the objective is infinite without simulating:
     // the reference rejects such answers afterwards (minimization.py:267), and
     // simulating there (e.g. mu_s' of 1e4 /cm: ~1e5 steps per packet) would
-    // stall the whole batched round
-    if (mua < r.lo[0] || mua > r.hi[0] || musr < r.lo[1] || musr > r.hi[1]) return 0;
+    // stall the whole batched round.  An initial guess outside the box (the
+    // reference's own example starts at (5, 45) for a [1,3] x [20,40] box)
+    // widens the evaluated region on that side to take it in, with margin,
+    // so that the search can walk from the guess into the box.
+    const double elo0 = r.x0[0] < r.lo[0] ? r.x0[0] / 1.5 : r.lo[0];
+    const double ehi0 = r.x0[0] > r.hi[0] ? r.x0[0] * 1.5 : r.hi[0];
+    const double elo1 = r.x0[1] < r.lo[1] ? r.x0[1] / 1.5 : r.lo[1];
+    const double ehi1 = r.x0[1] > r.hi[1] ? r.x0[1] * 1.5 : r.hi[1];
+    if (mua < elo0 || mua > ehi0 || musr < elo1 || musr > ehi1) return 0;
     ismc_instance base = r.base;
     const uint32_t l = r.layer;
     const double g = base.stack.g[l];

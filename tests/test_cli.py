@@ -151,3 +151,18 @@ def test_minimize_program_stdout_protocol(programs):
     assert abs(mua_hat / mua - 1) < 0.1, tok
     assert abs(mus_hat / mus_ - 1) < 0.05, tok
     assert mua_se >= 0 and mus_se >= 0
+
+
+@pytest.mark.gpu
+def test_minimize_program_reference_example(programs):
+    """The reference's own example configuration (--example: initial guess
+    (5, 45) outside its accepted box [1, 3] x [20, 40], separate spheres,
+    1e4 packets per objective, 5 runs) completes with an answer in the box."""
+    _, minimize = programs
+    r = _run([minimize, "--GPU", "0", "--example", "--go", "--seed", "11"])
+    assert r.returncode == 0, r.stdout + r.stderr
+    line = [l for l in r.stdout.splitlines() if l.startswith("mua:")]
+    assert line, r.stdout
+    mua = float(line[0].split()[1])
+    mus = float([l for l in r.stdout.splitlines() if l.startswith("mus':")][0].split()[1])
+    assert 1.0 <= mua <= 3.0 and 20.0 <= mus <= 40.0, r.stdout
