@@ -166,3 +166,19 @@ def test_minimize_program_reference_example(programs):
     mua = float(line[0].split()[1])
     mus = float([l for l in r.stdout.splitlines() if l.startswith("mus':")][0].split()[1])
     assert 1.0 <= mua <= 3.0 and 20.0 <= mus <= 40.0, r.stdout
+
+
+@pytest.mark.gpu
+def test_lookup_program_reference_example(programs, tmp_path):
+    """The reference's example table (--example: 13 x 11 grid, 1e5 packets,
+    10 runs, separate spheres) writes both CSVs with finite averages and
+    standard errors, R_d falling with mu_a along every mu_s' column."""
+    lookup, _ = programs
+    r = _run([lookup, "--GPU", "0", "--example", "--go", "--seed", "5"], cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    Rm, Rse = _read_like_lookup_py(tmp_path / "Diffuse_Reflectance.csv", 13)
+    Tm, Tse = _read_like_lookup_py(tmp_path / "Diffuse_Transmittance.csv", 13)
+    assert Rm.shape == (13, 11) and Tm.shape == (13, 11)
+    assert np.all(np.isfinite(Rm)) and np.all(np.isfinite(Tm))
+    assert np.all(Rse > 0) and np.all(Rse < 0.01) and np.all(Tse < 0.01)
+    assert np.all(np.diff(Rm, axis=0) < 0)
