@@ -179,6 +179,40 @@ def cpu_solve_baseline(engine, seconds=60.0, packets=100_000):
             "rel_err_vs_truth_median": np.median(np.array(errs), 0).tolist()}
 
 
+def cpu_tables_baseline(data, N=1000, M=100, cells_sample=300, seed=3):
+    """The reference's makelookup on the host (lookup.py:301-376): scipy's cubic
+    griddata for the four tables (timed in full), and the Python Monte Carlo
+    uncertainty loop restated in oracle/table64.py, timed on a sample of the
+    covered cells and scaled to all of them (the full loop runs for hours)."""
+    import numpy as np
+    from scipy.interpolate import griddata
+    import oracle.table64 as t64
+    Rd, Rs, Td, Ts, mu_a, mus_r = data
+    I, J = np.meshgrid(np.arange(1, Rd.shape[0]), np.arange(1, Rd.shape[1]), indexing="ij")
+    R, T = 100 * Rd[I, J].ravel(), 100 * Td[I, J].ravel()
+    o = np.lexsort((T, R))
+    P = np.stack([R[o], T[o]], 1)
+    g = np.linspace(0, 100, N)
+    GX, GY = np.meshgrid(g, g, indexing="ij")
+    t0 = time.perf_counter()
+    tabs = [griddata(P, v[o], (GX, GY), method="cubic") for v in
+            (mu_a[I].ravel(), mus_r[J].ravel(), 100 * Rs[I, J].ravel(), 100 * Ts[I, J].ravel())]
+    t_grid = time.perf_counter() - t0
+    ok = np.argwhere(np.isfinite(tabs[2]) & np.isfinite(tabs[3]) & (tabs[2] >= 0) & (tabs[3] >= 0))
+    rng = np.random.default_rng(seed)
+    pick = ok[rng.choice(len(ok), size=min(cells_sample, len(ok)), replace=False)]
+    t1 = time.perf_counter()
+    t64.uncertainty_map(tabs[0], tabs[1], tabs[2], tabs[3], M, seed,
+                        cells=[(int(i), int(j)) for i, j in pick])
+    per_cell = (time.perf_counter() - t1) / max(len(pick), 1)
+    total = t_grid + per_cell * len(ok)
+    return {"value": total, "unit": "s", "cores": 1, "kind": "port",
+            "sample": f"scipy griddata(cubic) x4 at {N}x{N}: {t_grid:.1f} s measured; uncertainty "
+                      f"loop (M={M}) measured on {len(pick)} of {len(ok)} cells, "
+                      f"{per_cell * 1e3:.2f} ms per cell, scaled",
+            "griddata_s": t_grid, "uncertainty_s_scaled": per_cell * len(ok)}
+
+
 def load_roofline_profile():
     try:
         with open(ROOFLINE_FILE) as fh:
@@ -342,6 +376,18 @@ def run_other_workload(args):
     build.build()
     eng = Engine(0)
     s = args.scale
+    if args.workload == "tables":
+        r, data = benchmarks.run_tables(eng, grid=max(8, int(64 * min(1.0, s))),
+                                        N=max(50, int(1000 * min(1.0, s))), M=100)
+        cpu = None if args.no_cpu_baseline else cpu_tables_baseline(data, N=r["N"], M=r["M"])
+        line = {"metric": "lookup-table inversion time", "value": r["tables_s"], "unit": "s",
+                "higher_is_better": False, "workload": "tables",
+                "config": {"workload": "grid x grid single-slab lookup (1e5 packets x 4 runs), then "
+                                       "makelookup: 4 Clough-Tocher N x N tables + M-draw "
+                                       "uncertainty map", "scale": s},
+                "cpu_baseline": cpu, "result": r}
+        print(json.dumps(line), flush=True)
+        return
     if args.workload == "lookup":
         r = benchmarks.run_lookup(eng, scale=s)
         line = {"metric": "photons/s", "value": r["photons_per_s"], "unit": "photons/s",
@@ -377,7 +423,7 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--packets", type=int, default=PACKETS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["forward", "lookup", "surrogate", "solve"],
+    ap.add_argument("--workload", choices=["forward", "lookup", "tables", "surrogate", "solve"],
                     default="forward")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="size factor for the secondary workloads (1 = full benchmark size)")

@@ -40,6 +40,30 @@ def run_lookup(engine: Engine, scale=1.0, seed=2, tune=None):
             "statuses_ok": all(r.status == 0 for r in res)}
 
 
+def run_tables(engine, grid=64, N=1000, M=100, packets=100_000, runs=4, seed=3):
+    """Lookup-table inversion at the reference's sizes (lookup.py:301-465 with
+    dimensions = 1000 and M = 100): a grid x grid lookup generated in one
+    launch, then the four Clough-Tocher tables and the Monte Carlo uncertainty
+    map on the GPU.  Returns timings and the inputs (for a CPU comparison)."""
+    from .api import Layer
+    from .lookup import interp_table, make_lookup, sample_space
+    mu_a = np.logspace(np.log10(0.01), np.log10(10.0), grid)
+    mus_r = np.logspace(0.0, 2.0, grid)
+    sl = (Layer.slide(1.5, 0.1), Layer.slide(1.5, 0.1))
+    t0 = time.perf_counter()
+    Rd, Rs, Td, Ts = sample_space(mu_a, mus_r, 0.9, 0.1, 1.4, bench_spheres(), packets, runs=runs,
+                                  separate=True, seed=seed, slides=sl, engine=engine)
+    t_gen = time.perf_counter() - t0
+    make_lookup(Rd[:8, :8], Td[:8, :8], Rs[:8, :8], Ts[:8, :8], mu_a[:8], mus_r[:8], N=64, M=8)
+    t1 = time.perf_counter()
+    mua_t, ua, mus_t, us, _, _ = make_lookup(Rd, Td, Rs, Ts, mu_a, mus_r, N=N, M=M, seed=seed)
+    t_tab = time.perf_counter() - t1
+    return {"grid": grid, "N": N, "M": M, "packets": packets, "runs": runs,
+            "generation_s": t_gen, "tables_s": t_tab,
+            "cells": N * N, "covered_cells": int(np.isfinite(mua_t).sum()),
+            "uncertainty_cells": int(np.isfinite(ua).sum())}, (Rd, Rs, Td, Ts, mu_a, mus_r)
+
+
 def make_measurements(engine, n, seed=4, packets=1_000_000, g=0.9, d=0.1, nidx=1.4,
                       noise=(0.002, 0.002, 0.0005)):
     """Synthetic measurements: MC at true (mu_a, mu_s') log-uniform over the

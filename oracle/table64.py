@@ -36,15 +36,17 @@ def find_nearest(grid, v):
     return int(np.abs(np.asarray(grid) - v).argmin())
 
 
-def uncertainty_map(mua, mus, rstd, tstd, M, seed):
-    """mua/mus/rstd/tstd: [N x N] tables indexed [R_i][T_j] (percent grid)."""
+def uncertainty_map(mua, mus, rstd, tstd, M, seed, cells=None):
+    """mua/mus/rstd/tstd: [N x N] tables indexed [R_i][T_j] (percent grid).
+    cells: optional (i, j) pairs to evaluate (the others stay NaN)."""
     N = mua.shape[0]
     grid = np.linspace(0, 100, N)
     k0, k1 = seed & MASK, (seed >> 32) & MASK
     ua = np.full((N, N), np.nan)
     us = np.full((N, N), np.nan)
-    for i in range(N):
-        for j in range(N):
+    todo = cells if cells is not None else ((i, j) for i in range(N) for j in range(N))
+    for i, j in todo:
+        if True:
             sR, sT = rstd[i, j], tstd[i, j]
             if np.isnan(sR) or np.isnan(sT) or sR < 0 or sT < 0:
                 continue
