@@ -15,7 +15,8 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from .api import IsmcError, Layer, Spheres, default_engine, load_library, make_instance
+from .api import (IsmcError, Layer, Spheres, default_engine, load_library, make_instance,
+                  tallies_mean_se)
 
 
 def _slab(n, mua, mus, g, t, slides):
@@ -25,39 +26,73 @@ def _slab(n, mua, mus, g, t, slides):
     return [slides[0], tissue, slides[1]]
 
 
-def _grid_instances(mu_a, mu_s_reduced, g, t, n, spheres, N, runs, separate, seed, stream0,
-                    slides, mode):
-    """Instances of one sample_space grid; Philox streams stream0, stream0+1, ...
-    in (mu_a, mu_s', repeat, sphere) order, so a grid run alone or inside a
-    larger batch gives the same tallies."""
+_KIND_R, _KIND_T, _KIND_RT = 0, 1, 2
+
+
+def _grid_fill(v, mu_a, mu_s_reduced, g, t, n, spheres, N, runs, separate, seed, stream0,
+               slides, mode):
+    """Fill v (a numpy view of consecutive ismc_instance entries) with one
+    sample_space grid, in (mu_a, mu_s', repeat, sphere) order with Philox
+    streams stream0, stream0+1, ..., so a grid run alone or inside a larger
+    batch gives the same tallies.  Returns the (i, j, repeat, kind) index."""
+    mu_a = np.asarray(mu_a, dtype=float)
     musr = np.asarray(mu_s_reduced, dtype=float)
     mus = musr / (1 - g) if g != 1 else musr          # lookup.py:236
     thr = 1e-3 if slides is None else 1e-4
-    sp_R = Spheres(**{**spheres.__dict__, "T": False})
-    sp_T = Spheres(**{**spheres.__dict__, "R": False})
-    insts, index = [], []
-    stream = stream0
-    for i, a in enumerate(np.asarray(mu_a, dtype=float)):
-        for j, s in enumerate(mus):
-            layers = _slab(n, float(a), float(s), g, t, slides)
-            for r in range(runs):
-                kinds = (("R", sp_R), ("T", sp_T)) if separate else (("RT", spheres),)
-                for which, sp in kinds:
-                    insts.append(make_instance(layers, sp, N, seed=seed, stream=stream,
-                                               mode=mode, roulette_threshold=thr))
-                    index.append((i, j, r, which))
-                    stream += 1
-    return insts, index
+    if separate:
+        kinds = ((_KIND_R, Spheres(**{**spheres.__dict__, "T": False})),
+                 (_KIND_T, Spheres(**{**spheres.__dict__, "R": False})))
+    else:
+        kinds = ((_KIND_RT, spheres),)
+    K, na, ns = len(kinds), len(mu_a), len(mus)
+    rows = np.arange(na * ns * runs * K)
+    i = rows // (ns * runs * K)
+    j = (rows // (runs * K)) % ns
+    r = (rows // K) % runs
+    k = rows % K
+    li = 0 if slides is None else 1                   # the tissue layer
+    for kk, (code, sp) in enumerate(kinds):
+        tmpl = (_abi.Instance * 1)(make_instance(_slab(n, float(mu_a[0]), float(mus[0]), g, t, slides),
+                                                 sp, N, seed=seed, stream=0, mode=mode,
+                                                 roulette_threshold=thr))
+        v[k == kk] = np.ctypeslib.as_array(tmpl)[0]
+    st = v["stack"]
+    st["mua"][:, li] = mu_a[i]
+    st["mus"][:, li] = mus[j]
+    st["mut"][:, li] = mu_a[i] + mus[j]
+    v["stream"] = (rows.astype(np.uint64) + np.uint64(stream0)) & np.uint64(0xFFFFFFFF)
+    which = np.array([c for c, _ in kinds])[k]
+    return {"i": i, "j": j, "r": r, "which": which}
+
+
+def _grid_instances(mu_a, mu_s_reduced, g, t, n, spheres, N, runs, separate, seed, stream0,
+                    slides, mode):
+    """The instances of one sample_space grid (a ctypes array) and their index."""
+    count = len(mu_a) * len(mu_s_reduced) * runs * (2 if separate else 1)
+    arr = (_abi.Instance * count)()
+    index = _grid_fill(np.ctypeslib.as_array(arr), mu_a, mu_s_reduced, g, t, n, spheres, N, runs,
+                       separate, seed, stream0, slides, mode)
+    return arr, index
 
 
 def _grid_tables(res, index, shape):
+    """R_d and T_d of every (mu_a, mu_s', repeat) from the batch's results
+    (a ctypes tally array or a list of Result)."""
+    if isinstance(res, C.Array):
+        mean = tallies_mean_se(res)[0]
+    else:
+        mean = np.array([x.mean for x in res], dtype=float)
+    return _grid_tables_from_mean(mean, index, shape)
+
+
+def _grid_tables_from_mean(mean, index, shape):
     Rd = np.zeros(shape)
     Td = np.zeros(shape)
-    for (i, j, r, which), x in zip(index, res):
-        if which in ("R", "RT"):
-            Rd[i, j, r] = x.mean[1]
-        if which in ("T", "RT"):
-            Td[i, j, r] = x.mean[3]
+    i, j, r, w = index["i"], index["j"], index["r"], index["which"]
+    m = w != _KIND_T
+    Rd[i[m], j[m], r[m]] = mean[m, 1]
+    m = w != _KIND_R
+    Td[i[m], j[m], r[m]] = mean[m, 3]
     return Rd, Td
 
 
@@ -71,7 +106,7 @@ def sample_space(mu_a, mu_s_reduced, g, t, n, spheres: Spheres, N, runs=1, separ
     eng = engine or default_engine()
     insts, index = _grid_instances(mu_a, mu_s_reduced, g, t, n, spheres, N, runs, separate, seed,
                                    0, slides, mode)
-    Rd, Td = _grid_tables(eng.run_batch(insts, tune), index,
+    Rd, Td = _grid_tables(eng.run_batch_raw(insts, tune), index,
                           (len(mu_a), len(mu_s_reduced), runs))
     return Rd.mean(-1), Rd.std(-1), Td.mean(-1), Td.std(-1)
 
@@ -103,21 +138,20 @@ def run_uncertainty(mu_a, mu_s_reduced, g, t, samples, N, runs=1, separate=True,
     samples of R_d and T_d and their spread: sqrt(sum of per-sample repeat
     variances) when runs > 1, else the standard deviation over samples."""
     eng = engine or default_engine()
-    insts, index, slices = [], [], []
     per = len(mu_a) * len(mu_s_reduced) * runs * (2 if separate else 1)
-    for r, (n_r, sph_r) in enumerate(samples):
-        a, b = _grid_instances(mu_a, mu_s_reduced, g, t, n_r, sph_r, N, runs, separate, seed,
-                               r * per, slides, mode)
-        slices.append((len(insts), len(insts) + len(a)))
-        insts += a
-        index += b
-    res = eng.run_batch(insts, tune)
+    arr = (_abi.Instance * (per * len(samples)))()
+    v = np.ctypeslib.as_array(arr)
+    indices = [_grid_fill(v[r * per:(r + 1) * per], mu_a, mu_s_reduced, g, t, n_r, sph_r, N, runs,
+                          separate, seed, r * per, slides, mode)
+               for r, (n_r, sph_r) in enumerate(samples)]
+    res = eng.run_batch_raw(arr, tune)
     O = len(samples)
     shape = (len(mu_a), len(mu_s_reduced), runs)
     Rd, Td = np.zeros((O,) + shape[:2]), np.zeros((O,) + shape[:2])
     Rv, Tv = np.zeros(shape[:2]), np.zeros(shape[:2])
-    for r, (lo, hi) in enumerate(slices):
-        R3, T3 = _grid_tables(res[lo:hi], index[lo:hi], shape)
+    mean = tallies_mean_se(res)[0]
+    for r, index in enumerate(indices):
+        R3, T3 = _grid_tables_from_mean(mean[r * per:(r + 1) * per], index, shape)
         Rd[r], Td[r] = R3.mean(-1), T3.mean(-1)
         Rv += R3.std(-1) ** 2
         Tv += T3.std(-1) ** 2

@@ -44,3 +44,41 @@ def test_tallies_mean_se_matches_tally_to_result():
                 assert np.isnan(mean[i, k]) and np.isnan(se[i, k])
             else:
                 assert mean[i, k] == r.mean[k] and se[i, k] == r.se[k], (i, k)
+
+
+def _grid_loop(mu_a, musr, g, t, n, spheres, N, runs, separate, seed, stream0, slides, mode):
+    """The one-instance-at-a-time construction the vectorised grid builder replaces."""
+    from ismc_gb300 import Layer, Spheres
+    mus = np.asarray(musr, float) / (1 - g) if g != 1 else np.asarray(musr, float)
+    thr = 1e-3 if slides is None else 1e-4
+    sp_R = Spheres(**{**spheres.__dict__, "T": False})
+    sp_T = Spheres(**{**spheres.__dict__, "R": False})
+    out, stream = [], stream0
+    for a in np.asarray(mu_a, float):
+        for s in mus:
+            tissue = Layer(n, float(a), float(s), g, t)
+            layers = [tissue] if slides is None else [slides[0], tissue, slides[1]]
+            for _ in range(runs):
+                for sp in ((sp_R, sp_T) if separate else (spheres,)):
+                    out.append(api.make_instance(layers, sp, N, seed=seed, stream=stream, mode=mode,
+                                                 roulette_threshold=thr))
+                    stream += 1
+    return out
+
+
+def test_grid_instances_are_byte_identical_to_the_loop():
+    from ismc_gb300 import Layer
+    from ismc_gb300.lookup import _grid_instances
+    mu_a = 0.5 * 1.2 ** np.arange(5)
+    musr = 10 * 1.3 ** np.arange(4)
+    sph = bench_spheres()
+    for slides in (None, (Layer.slide(1.5, 0.1), Layer.slide(1.52, 0.12))):
+        for separate, runs in ((True, 2), (False, 3)):
+            arr, index = _grid_instances(mu_a, musr, 0.9, 0.135, 1.41, sph, 7777, runs, separate,
+                                         12, 500, slides, "compat")
+            ref = _grid_loop(mu_a, musr, 0.9, 0.135, 1.41, sph, 7777, runs, separate, 12, 500,
+                             slides, "compat")
+            assert len(arr) == len(ref)
+            for a, b in zip(arr, ref):
+                assert bytes(a) == bytes(b)
+            assert index["i"].max() == 4 and index["j"].max() == 3 and index["r"].max() == runs - 1
