@@ -213,6 +213,14 @@ def cpu_tables_baseline(data, N=1000, M=100, cells_sample=300, seed=3):
             "griddata_s": t_grid, "uncertainty_s_scaled": per_cell * len(ok)}
 
 
+def load_measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
 def load_roofline_profile():
     try:
         with open(ROOFLINE_FILE) as fh:
@@ -349,6 +357,13 @@ def run_gpu(args, rank, world, dist):
                     source=os.path.relpath(ROOFLINE_FILE, ROOT))
     else:
         roof.update(steps_per_s=steps_per_s)
+    # the HBM side, for completeness: DRAM bytes per launch (ncu) over the launch
+    # time, against the measured copy bandwidth
+    peaks = load_measured_peaks()
+    if prof and prof.get("dram_bytes_per_launch") and peaks.get("hbm_gbs"):
+        gbs = prof["dram_bytes_per_launch"] / (dev_time / args.steps) / 1e9
+        roof["hbm"] = {"achieved_gbs": gbs, "peak_gbs": peaks["hbm_gbs"],
+                       "frac": gbs / peaks["hbm_gbs"], "peak_source": "MEASURED_PEAKS.json (of measured)"}
     cpu = cpu_baseline() if (world == 1 and not args.no_cpu_baseline) else None
     line = {"metric": "photons/s", "value": value, "unit": "photons/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dev_time / args.steps,
