@@ -213,6 +213,42 @@ def cpu_tables_baseline(data, N=1000, M=100, cells_sample=300, seed=3):
             "griddata_s": t_grid, "uncertainty_s_scaled": per_cell * len(ok)}
 
 
+def cpu_lookup_baseline(r, seconds=20.0, sample=64):
+    """The FP64 restatement of the reference on a stratified sample of the
+    lookup workload's instances (every k-th of the 4608, budgets capped so the
+    sample takes about `seconds`), on all host cores; the full workload's CPU
+    time is extrapolated from its photon-step count."""
+    import copy
+    import oracle
+    from ismc_gb300.workloads import lookup_grid
+    insts = lookup_grid(seed=2, scale=r.get("scale", 1.0))
+    stride = max(1, len(insts) // sample)
+    pick = [copy.copy(insts[i]) for i in range(0, len(insts), stride)][:sample]
+    threads = os.cpu_count()
+    cap = 2000
+    t0 = time.perf_counter()
+    for x in pick[:8]:
+        x2 = copy.copy(x)
+        x2.n_packets = min(int(x.n_packets), cap)
+        oracle.ref64_run(x2, threads=threads)
+    per = (time.perf_counter() - t0) / 8
+    cap = max(1000, int(cap * seconds / max(per * len(pick), 1e-3)))
+    packets = steps = 0
+    t0 = time.perf_counter()
+    for x in pick:
+        x.n_packets = min(int(x.n_packets), cap)
+        _, _, st = oracle.ref64_run(x, threads=threads)
+        packets += int(x.n_packets)
+        steps += st
+    dt = time.perf_counter() - t0
+    sps = steps / dt
+    return {"value": packets / dt, "unit": "photons/s", "cores": threads, "kind": "port",
+            "steps_per_s": sps,
+            "sample": f"{len(pick)} instances (every {stride}th of the workload), at most {cap} packets "
+                      f"each, FP64 C restatement on {threads} threads, {dt:.1f} s",
+            "full_workload_s_extrapolated": r["steps_per_s"] * r["seconds"] / sps}
+
+
 def load_measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -405,8 +441,10 @@ def run_other_workload(args):
         return
     if args.workload == "lookup":
         r = benchmarks.run_lookup(eng, scale=s)
+        r["scale"] = s
+        cpu = None if args.no_cpu_baseline else cpu_lookup_baseline(r)
         line = {"metric": "photons/s", "value": r["photons_per_s"], "unit": "photons/s",
-                "workload": "lookup", "config": {"workload": "64x64 single-slab grid + 512 random "
+                "workload": "lookup", "cpu_baseline": cpu, "config": {"workload": "64x64 single-slab grid + 512 random "
                 "1-5 layer stacks, budgets log-uniform 1e5-1e7 x scale, one persistent launch",
                 "scale": s}, "result": r}
     else:
