@@ -249,6 +249,41 @@ def cpu_lookup_baseline(r, seconds=20.0, sample=64):
             "full_workload_s_extrapolated": r["steps_per_s"] * r["seconds"] / sps}
 
 
+def run_dropin_workload(calls=200, N=10_000):
+    """The reference's Python drivers call ISMC() once per grid point or
+    objective (lookup.py:238, minimization.py:205).  Times that call through
+    the drop-in module (GPU) for the config-0 slab, and the same call on the
+    FP64 restatement of ISMC.py on one core (the reference's Python is serial)."""
+    import oracle
+    import ismc_gb300.dropin.ISMC as D
+    from ismc_gb300 import make_instance
+    from ismc_gb300.workloads import bench_spheres
+    sp = bench_spheres()
+    args = (1.4, 0.9, 0.1, 1.0, 100.0, 101.0, True, sp.R_pw, sp.R_fs, sp.R_fp, sp.R_fd, sp.R_f,
+            sp.R_angle, False, True, sp.T_pw, sp.T_fs, sp.T_fp, sp.T_fd, sp.T_f, sp.T_angle)
+    for _ in range(5):
+        D.ISMC(N, *args)
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        D.ISMC(N, *args)
+    dt = (time.perf_counter() - t0) / calls
+    from ismc_gb300 import Layer
+    inst = make_instance([Layer(1.4, 1.0, 100.0, 0.9, 0.1, 101.0)], sp, N, seed=1,
+                         roulette_threshold=1e-3)
+    t0 = time.perf_counter()
+    oracle.ref64_run(inst, threads=1)
+    dt_cpu = time.perf_counter() - t0
+    line = {"metric": "ISMC() calls/s", "value": 1.0 / dt, "unit": "calls/s", "workload": "dropin",
+            "config": {"workload": "drop-in ISMC() on the bare config-0 slab (n 1.4, mu_a 1, "
+                                   "mu_s 100, g 0.9, d 0.1 cm), both spheres", "packets_per_call": N,
+                       "calls": calls},
+            "result": {"seconds_per_call": dt},
+            "cpu_baseline": {"value": 1.0 / dt_cpu, "unit": "calls/s", "cores": 1, "kind": "port",
+                             "sample": f"one {N}-packet call of the FP64 restatement of ISMC.py, "
+                                       f"{dt_cpu:.2f} s"}}
+    print(json.dumps(line), flush=True)
+
+
 def load_measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -427,6 +462,9 @@ def run_other_workload(args):
     build.build()
     eng = Engine(0)
     s = args.scale
+    if args.workload == "dropin":
+        run_dropin_workload()
+        return
     if args.workload == "tables":
         r, data = benchmarks.run_tables(eng, grid=max(8, int(64 * min(1.0, s))),
                                         N=max(50, int(1000 * min(1.0, s))), M=100)
@@ -476,7 +514,8 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--packets", type=int, default=PACKETS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["forward", "lookup", "tables", "surrogate", "solve"],
+    ap.add_argument("--workload", choices=["forward", "lookup", "tables", "surrogate", "solve",
+                                           "dropin"],
                     default="forward")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="size factor for the secondary workloads (1 = full benchmark size)")
