@@ -344,23 +344,28 @@ extern "C" int ismc_autotune(ismc_ctx* ctx, const ismc_instance* inst, uint32_t 
     const uint64_t total = std::max<uint64_t>(1, total_packets(inst, n_inst));
     const double scale = std::min(1.0, 4.0e6 / (double)total);
     std::vector<ismc_instance> trial(inst, inst + n_inst);
-    uint64_t ttotal = 0;
-    for (auto& x : trial) {
-        x.n_packets = (uint64_t)((double)x.n_packets * scale + 0.5);
-        ttotal += x.n_packets;
-    }
+    for (auto& x : trial) x.n_packets = (uint64_t)((double)x.n_packets * scale + 0.5);
     rc = ensure_capacity(ctx, n_inst);
     if (rc) return rc;
     CK(cudaMemcpy(ctx->d_in, trial.data(), sizeof(ismc_instance) * n_inst, cudaMemcpyHostToDevice));
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
+    // events are destroyed and the context's chunking restored on every exit path
+    struct Trial {
+        ismc_ctx* c;
+        uint32_t saved_cpw;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        ~Trial() {
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+            c->chunks_per_warp = saved_cpw;
+        }
+    } tr{ctx, ctx->chunks_per_warp};
+    CK(cudaEventCreate(&tr.e0));
+    CK(cudaEventCreate(&tr.e1));
     const uint32_t threads_c[] = {128, 256, 512};
     const uint32_t cpw_c[] = {8, 32, 128};
     float best = 1e30f;
     ismc_tune best_t = ctx->tune;
     uint32_t best_cpw = ctx->chunks_per_warp;
-    const uint32_t saved_cpw = ctx->chunks_per_warp;
     for (uint32_t th : threads_c) {
         for (uint32_t cpw : cpw_c) {
             ismc_tune t{th, 0, 0, 0};
@@ -370,25 +375,19 @@ extern "C" int ismc_autotune(ismc_ctx* ctx, const ismc_instance* inst, uint32_t 
             ctx->chunks_per_warp = cpw;
             float best_ms = 1e30f;
             for (int rep = 0; rep < 2; ++rep) {
-                CK(cudaEventRecord(e0, ctx->stream));
+                CK(cudaEventRecord(tr.e0, ctx->stream));
                 rc = enqueue_pipeline(ctx, ctx->d_in, n_inst, r, blocks, ctx->d_out, ctx->stream);
-                if (rc) {
-                    ctx->chunks_per_warp = saved_cpw;
-                    cudaEventDestroy(e0);
-                    cudaEventDestroy(e1);
-                    return rc;
-                }
-                CK(cudaEventRecord(e1, ctx->stream));
-                CK(cudaEventSynchronize(e1));
+                if (rc) return rc;
+                CK(cudaEventRecord(tr.e1, ctx->stream));
+                CK(cudaEventSynchronize(tr.e1));
                 float ms = 0;
-                CK(cudaEventElapsedTime(&ms, e0, e1));
+                CK(cudaEventElapsedTime(&ms, tr.e0, tr.e1));
                 best_ms = std::min(best_ms, ms);
             }
             if (best_ms < best) { best = best_ms; best_t = t; best_cpw = cpw; }
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    tr.saved_cpw = best_cpw;
     // keep the winning block size and chunks-per-warp; the chunk size itself is
     // re-derived on the device from each batch's total packet count
     ctx->tune.block_threads = best_t.block_threads;
