@@ -10,10 +10,16 @@
 // shared memory by TMA (128-byte swizzle), multiplied by tcgen05.mma issued
 // from one thread into a TMEM accumulator (128 lanes x BN fp32 columns), and
 // read back by four warps with tcgen05.ld for a fused epilogue:
-//   EPI_HIDDEN  z = acc + b;  H = silu(z) (row- and column-major bf16), G = silu'(z)
-//   EPI_BWD     dz = acc * G  (row- and column-major bf16)
+//   EPI_HIDDEN  z = acc + b;  H = silu(z) (row- and column-major bf16),
+//               G = silu'(z) (column-major bf16)
+//   EPI_BWD     dz = acc * G  (row- and column-major bf16), and the bias
+//               gradient as column sums of dz
 //   EPI_OUT     z = acc + b   (fp32)
 //   EPI_ACC     atomicAdd(acc) into fp32 (split-K weight gradients)
+// Each block of up to 64 columns is staged in the freed operand buffers, so
+// row-major outputs are written as whole 16-byte vectors and the split-K
+// gradients as coalesced atomics; column-major outputs are coalesced as
+// written (consecutive threads hold consecutive rows).
 // Layer inputs are padded to K = 64 and the output layer to 16 rows, so every
 // product uses the same 64-wide K chunks.
 #include <cuda.h>
@@ -42,20 +48,22 @@ struct Epi {
     int mode;
     int M, N;                      // valid rows / columns of D
     const float* bias;             // [N]
-    const __nv_bfloat16* gate;     // [M x ldg] (EPI_BWD)
+    const __nv_bfloat16* gate;     // [N x ldg] column-major silu'(z) (EPI_BWD)
     int ldg;
+    float* bias_grad;              // [N] += column sums of dz (EPI_BWD, optional)
     __nv_bfloat16* out_row;        // [M x ldr]
     int ldr;
     __nv_bfloat16* out_col;        // [N x ldc] (transposed copy)
     int ldc;
-    __nv_bfloat16* out_aux;        // [M x lda]  silu'(z)
+    __nv_bfloat16* out_aux;        // [N x lda] column-major silu'(z)
     int lda;
     float* out_f;                  // [M x ldf]
     int ldf;
     int fold;                      // EPI_ACC: column n accumulates into n % fold (0: n)
 };
 
-__device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + __expf(-z)); }
+// 1 / (1 + e^-z); the fast divide returns 0 once e^-z passes 2^126, the limit anyway
+__device__ __forceinline__ float sigmoidf_(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 
 template <int BN>
 __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ CUtensorMap tA,
@@ -91,6 +99,9 @@ __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ 
     __syncthreads();
     umma::fence_after_sync();
     const uint32_t tmem = *tslot;
+    // Launched with programmatic stream serialisation, the set-up above overlaps
+    // the previous product's tail; every global access comes after this wait.
+    umma::grid_dep_wait();
 
     if (threadIdx.x == 0) {
         const uint32_t sa0 = umma::smem_u32(smem), sb0 = sa0 + A_BYTES;
@@ -129,50 +140,104 @@ __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ 
     __syncthreads();
     bool ok = *sfail == 0;
     if (ok) ok = umma::mbar_wait(umma::smem_u32(bars + 4), 0, WAIT_LIMIT);
+    // one verdict for the block: the epilogue below synchronises the block
+    ok = __syncthreads_and(ok) != 0;
+    // the operands are consumed: the next product may start its set-up
+    umma::grid_dep_launch();
     if (!ok) {
         if (threadIdx.x == 0) atomicExch(err, 1);
     } else {
         umma::fence_after_sync();
-        const int r = m0 + warp * 32 + lane;                 // this thread's row
+        // The last MMA has read the operand stages, so blocks of CB columns are
+        // staged there: bf16 rows of SB elements (hidden / backward) or fp32
+        // rows of SF (output / gradient), padded so that the 16-byte row writes
+        // of consecutive threads fall in distinct banks.
+        constexpr int CB = BN < 64 ? BN : 64;
+        constexpr int SB = CB + 8, SF = CB + 4;
+        static_assert(BN % CB == 0 && BM % CB == 0, "column blocks");
+        static_assert((size_t)BM * SF * 4 <= 2 * (size_t)STAGE, "staging fits the operand stages");
+        __nv_bfloat16* sb = reinterpret_cast<__nv_bfloat16*>(smem);
+        float* sf = reinterpret_cast<float*>(smem);
+        const int rl = warp * 32 + lane;                     // this thread's row of the tile
+        const int r = m0 + rl;
         const bool row_ok = r < e.M;
+        const bool bf = e.mode == EPI_HIDDEN || e.mode == EPI_BWD;
 #pragma unroll 1
-        for (int c = 0; c < BN; c += 16) {
-            float v[16];
-            umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
-            const int nb = n0 + c;
-            if (!row_ok) continue;
+        for (int cb = 0; cb < BN; cb += CB) {
+#pragma unroll 1
+            for (int c = 0; c < CB; c += 16) {
+                float v[16];
+                umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb + c), v);
+                const int nb = n0 + cb + c;
+                if (bf) {
+                    __align__(16) __nv_bfloat16 o[16];
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int n = nb + j;
-                if (n >= e.N) break;
-                float x = v[j];
-                switch (e.mode) {
-                    case EPI_HIDDEN: {
-                        const float z = x + e.bias[n];
-                        const float sg = sigmoidf_(z);
-                        const float h = z * sg;
-                        const __nv_bfloat16 hb = __float2bfloat16_rn(h);
-                        e.out_row[(size_t)r * e.ldr + n] = hb;
-                        e.out_col[(size_t)n * e.ldc + r] = hb;
-                        e.out_aux[(size_t)r * e.lda + n] =
-                            __float2bfloat16_rn(sg * (1.0f + z * (1.0f - sg)));
-                        break;
+                    for (int j = 0; j < 16; ++j) {
+                        const int n = nb + j;
+                        const bool ok = row_ok && n < e.N;
+                        __nv_bfloat16 b = __float2bfloat16_rn(0.0f);
+                        if (ok && e.mode == EPI_HIDDEN) {
+                            const float z = v[j] + e.bias[n];
+                            const float sg = sigmoidf_(z);
+                            b = __float2bfloat16_rn(z * sg);
+                            e.out_col[(size_t)n * e.ldc + r] = b;
+                            e.out_aux[(size_t)n * e.lda + r] =
+                                __float2bfloat16_rn(sg * (1.0f + z * (1.0f - sg)));
+                        } else if (ok) {
+                            b = __float2bfloat16_rn(v[j] * __bfloat162float(e.gate[(size_t)n * e.ldg + r]));
+                            e.out_col[(size_t)n * e.ldc + r] = b;
+                        }
+                        o[j] = b;
                     }
-                    case EPI_BWD: {
-                        const float dz = x * __bfloat162float(e.gate[(size_t)r * e.ldg + n]);
-                        const __nv_bfloat16 b = __float2bfloat16_rn(dz);
-                        e.out_row[(size_t)r * e.ldr + n] = b;
-                        e.out_col[(size_t)n * e.ldc + r] = b;
-                        break;
+                    uint4* dst = reinterpret_cast<uint4*>(sb + rl * SB + c);
+                    dst[0] = reinterpret_cast<const uint4*>(o)[0];
+                    dst[1] = reinterpret_cast<const uint4*>(o)[1];
+                } else {
+                    if (e.mode == EPI_OUT) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            if (nb + j < e.N) v[j] += e.bias[nb + j];
                     }
-                    case EPI_OUT:
-                        e.out_f[(size_t)r * e.ldf + n] = x + e.bias[n];
-                        break;
-                    default:
-                        atomicAdd(e.out_f + (size_t)r * e.ldf + (e.fold ? n % e.fold : n), x);
-                        break;
+                    float4* dst = reinterpret_cast<float4*>(sf + rl * SF + c);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
                 }
             }
+            __syncthreads();
+            if (bf) {
+                // row-major copy: CB / 8 16-byte vectors per row (N is a multiple of CB here)
+                constexpr int VPR = CB / 8;
+                for (int idx = threadIdx.x; idx < BM * VPR; idx += blockDim.x) {
+                    const int row = idx / VPR, q = idx % VPR;
+                    const int gr = m0 + row, gn = n0 + cb + q * 8;
+                    if (gr < e.M && gn < e.N)
+                        *reinterpret_cast<uint4*>(e.out_row + (size_t)gr * e.ldr + gn) =
+                            *reinterpret_cast<const uint4*>(sb + row * SB + q * 8);
+                }
+                if (e.mode == EPI_BWD && e.bias_grad) {
+                    // column sums of the rounded dz over the tile's rows (rows past M are 0)
+                    constexpr int PARTS = 128 / CB, RPP = BM / PARTS;
+                    const int col = threadIdx.x % CB, part = threadIdx.x / CB;
+                    if (threadIdx.x < CB * PARTS && n0 + cb + col < e.N) {
+                        float acc = 0.0f;
+                        for (int row = part * RPP; row < (part + 1) * RPP; ++row)
+                            acc += __bfloat162float(sb[row * SB + col]);
+                        atomicAdd(e.bias_grad + n0 + cb + col, acc);
+                    }
+                }
+            } else {
+                for (int idx = threadIdx.x; idx < BM * CB; idx += blockDim.x) {
+                    const int row = idx / CB, col = idx % CB;
+                    const int gr = m0 + row, gn = n0 + cb + col;
+                    if (gr < e.M && gn < e.N) {
+                        const float x = sf[row * SF + col];
+                        if (e.mode == EPI_OUT) e.out_f[(size_t)gr * e.ldf + gn] = x;
+                        else atomicAdd(e.out_f + (size_t)gr * e.ldf + (e.fold ? gn % e.fold : gn), x);
+                    }
+                }
+            }
+            __syncthreads();
         }
     }
     umma::fence_before_sync();
@@ -196,26 +261,27 @@ struct Norm { float lo[5], hi[5]; };
 // column 5 + k; the first layer's weights are stored twice (columns k and
 // 5 + k), so the product sees f to about 16 bits instead of bf16's 8 and the
 // network is smooth in its inputs at the resolution the inverse solver needs.
-// Columns 10-63 are zero.
+// Columns 10-63 of X0 are zero from creation (this kernel writes columns 0-15
+// as two 16-byte vectors); rows 10-63 of X0T only ever meet gradient columns
+// that are not kept.
 __global__ void prep_inputs(const float* __restrict__ x, int B, Norm nm, __nv_bfloat16* X0,
                             __nv_bfloat16* X0T) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= B) return;
-    float f[5];
+    __align__(16) __nv_bfloat16 o[16];
 #pragma unroll
-    for (int k = 0; k < 5; ++k)
-        f[k] = 2.0f * (x[(size_t)r * 5 + k] - nm.lo[k]) / (nm.hi[k] - nm.lo[k]) - 1.0f;
-    for (int k = 0; k < 64; ++k) {
-        __nv_bfloat16 b = __float2bfloat16_rn(0.0f);
-        if (k < 5) {
-            b = __float2bfloat16_rn(f[k]);
-        } else if (k < 10) {
-            const float hi = __bfloat162float(__float2bfloat16_rn(f[k - 5]));
-            b = __float2bfloat16_rn(f[k - 5] - hi);
-        }
-        X0[(size_t)r * 64 + k] = b;
-        X0T[(size_t)k * B + r] = b;
+    for (int k = 0; k < 16; ++k) o[k] = __float2bfloat16_rn(0.0f);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const float f = 2.0f * (x[(size_t)r * 5 + k] - nm.lo[k]) / (nm.hi[k] - nm.lo[k]) - 1.0f;
+        o[k] = __float2bfloat16_rn(f);
+        o[5 + k] = __float2bfloat16_rn(f - __bfloat162float(o[k]));
     }
+    uint4* dst = reinterpret_cast<uint4*>(X0 + (size_t)r * 64);
+    dst[0] = reinterpret_cast<const uint4*>(o)[0];
+    dst[1] = reinterpret_cast<const uint4*>(o)[1];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) X0T[(size_t)k * B + r] = o[k];
 }
 
 // Gaussian NLL with a variance floor: out O [B x 16] fp32 (mu in cols 0-2,
@@ -225,70 +291,75 @@ __global__ void prep_inputs(const float* __restrict__ x, int B, Norm nm, __nv_bf
 // The floor (the training targets' Monte Carlo noise scale) keeps the
 // per-sample precision weights bounded where the targets are noise-free
 // (e.g. T_u = 0 for thick samples); floor = 0 is the plain Gaussian NLL.
-// dO (bf16 [B x 64] row, [64 x B] column; unused columns zero) = dloss/dO.
+// dO (bf16 [B x 64] row, [64 x B] column) = dloss/dO: columns 0-15 of dO are
+// written (6-15 as zeros; 16-63 stay zero from creation) and rows 0-5 of dOT.
+// The output layer's bias gradient db[k] = sum_b bf16(dO[b][k]) is reduced here
+// too (block sums, one atomic per block and column).
 __global__ void nll_loss_grad(const float* __restrict__ O, const float* __restrict__ y, int B,
                               float inv_b, float floor2, __nv_bfloat16* dO, __nv_bfloat16* dOT,
-                              float* loss) {
+                              float* loss, float* db) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    float l = 0.0f;
+    float part[7] = {0, 0, 0, 0, 0, 0, 0};      // loss, then the six bias-gradient columns
     if (r < B) {
-        for (int k = 0; k < 64; ++k) {
-            float g = 0.0f;
-            if (k < 6) {
-                const int q = k < 3 ? k : k - 3;
-                const float mu = O[(size_t)r * 16 + q], s = O[(size_t)r * 16 + 3 + q];
-                const float d = y[(size_t)r * 3 + q] - mu;
-                const float es = __expf(s);
-                const float v = es + floor2;
-                const float iv = 1.0f / v;
-                if (k < 3) {
-                    l += 0.5f * (d * d * iv + __logf(v));
-                    g = -d * iv * inv_b;
-                } else {
-                    g = 0.5f * es * iv * (1.0f - d * d * iv) * inv_b;
-                }
-            }
-            const __nv_bfloat16 b = __float2bfloat16_rn(g);
-            dO[(size_t)r * 64 + k] = b;
-            dOT[(size_t)k * B + r] = b;
+        __align__(16) __nv_bfloat16 o[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) o[k] = __float2bfloat16_rn(0.0f);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float mu = O[(size_t)r * 16 + q], s = O[(size_t)r * 16 + 3 + q];
+            const float d = y[(size_t)r * 3 + q] - mu;
+            const float es = __expf(s);
+            const float v = es + floor2;
+            const float iv = 1.0f / v;
+            part[0] += 0.5f * (d * d * iv + __logf(v));
+            o[q] = __float2bfloat16_rn(-d * iv * inv_b);
+            o[3 + q] = __float2bfloat16_rn(0.5f * es * iv * (1.0f - d * d * iv) * inv_b);
+        }
+        uint4* dst = reinterpret_cast<uint4*>(dO + (size_t)r * 64);
+        dst[0] = reinterpret_cast<const uint4*>(o)[0];
+        dst[1] = reinterpret_cast<const uint4*>(o)[1];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            dOT[(size_t)k * B + r] = o[k];
+            part[1 + k] = __bfloat162float(o[k]);
         }
     }
-    // block reduction of the loss
-    __shared__ float red[256];
-    red[threadIdx.x] = l;
+    // block reduction: warp shuffles, then one row of partial sums per warp
+    __shared__ float red[32][7];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 7; ++k)
+        for (int off = 16; off > 0; off >>= 1) part[k] += __shfl_down_sync(0xFFFFFFFFu, part[k], off);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 7; ++k) red[warp][k] = part[k];
     __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
+    if (threadIdx.x < 7) {
+        float t = 0.0f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][threadIdx.x];
+        if (threadIdx.x == 0) atomicAdd(loss, t * inv_b);
+        else atomicAdd(db + threadIdx.x - 1, t);
     }
-    if (threadIdx.x == 0) atomicAdd(loss, red[0] * inv_b);
 }
 
-// db[n] = sum_b dZT[n][b]  (one block per row n)
-__global__ void bias_grad(const __nv_bfloat16* __restrict__ dZT, int B, int N, float* db) {
-    const int n = blockIdx.x;
-    if (n >= N) return;
-    float s = 0.0f;
-    for (int b = threadIdx.x; b < B; b += blockDim.x) s += __bfloat162float(dZT[(size_t)n * B + b]);
-    __shared__ float red[256];
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) db[n] = red[0];
-}
+// The parameter tensors of one Adam step, in the flat buffers' order: each
+// has R x C fp32 entries from `off`, and optional bf16 copies used by the
+// GEMMs: W [R x ldw] (row, K-major for the forward; with dup > 0 also at
+// column c + dup, for the first layer's split inputs) and WT [C x ldt]
+// (transposed, K-major for the backward).
+struct AdamSeg {
+    int off, R, C, ldw, dup, ldt;
+    __nv_bfloat16* W;
+    __nv_bfloat16* WT;
+};
+struct AdamSegs { AdamSeg s[8]; int n; };
 
-// One parameter tensor: fp32 master w [R x C], gradient g, Adam moments m, v;
-// writes the bf16 copies used by the GEMMs: W [R x ldw] (row, K-major for the
-// forward; with dup > 0 also at column c + dup, for the first layer's split
-// inputs) and WT [C x ldt] (transposed, K-major for the backward).
-__global__ void adam_update(float* w, const float* g, float* m, float* v, int R, int C, float lr,
-                            float b1, float b2, float eps, float bc1, float bc2,
-                            __nv_bfloat16* W, int ldw, int dup, __nv_bfloat16* WT, int ldt) {
+// One Adam step of every parameter (fp32 master w, gradient g, moments m, v),
+// one thread per parameter, refreshing the bf16 copies.
+__global__ void adam_update(float* w, const float* g, float* m, float* v, int total, AdamSegs S,
+                            float lr, float b1, float b2, float eps, float bc1, float bc2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= R * C) return;
+    if (i >= total) return;
     const float gi = g[i];
     const float mi = b1 * m[i] + (1.0f - b1) * gi;
     const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
@@ -296,13 +367,16 @@ __global__ void adam_update(float* w, const float* g, float* m, float* v, int R,
     v[i] = vi;
     const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
     w[i] = wi;
-    const int r = i / C, c = i % C;
+    int k = 0;
+    while (k + 1 < S.n && i >= S.s[k + 1].off) ++k;
+    const AdamSeg& a = S.s[k];
+    const int j = i - a.off, r = j / a.C, c = j % a.C;
     const __nv_bfloat16 b = __float2bfloat16_rn(wi);
-    if (W) {
-        W[(size_t)r * ldw + c] = b;
-        if (dup) W[(size_t)r * ldw + c + dup] = b;
+    if (a.W) {
+        a.W[(size_t)r * a.ldw + c] = b;
+        if (a.dup) a.W[(size_t)r * a.ldw + c + a.dup] = b;
     }
-    if (WT) WT[(size_t)c * ldt + r] = b;
+    if (a.WT) a.WT[(size_t)c * a.ldt + r] = b;
 }
 
 // bf16 copies of a parameter tensor without an update
@@ -420,21 +494,35 @@ static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, 
     // A: [M x K] bf16, B: [N x K] bf16, both K-major; M % 128 == 0, N % BN == 0, K % 64 == 0
     if (M % BM || N % BN || K % (BK * splits))
         return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: shape not tileable");
+    // bf16 row-major outputs leave as 16-byte vectors of 8 columns
+    if ((e.mode == EPI_HIDDEN || e.mode == EPI_BWD) && (e.N % 8 || e.ldr % 8))
+        return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: row-major output not 16-byte tileable");
     CUtensorMap ta, tb;
     int rc = get_map(m, &ta, A, (uint64_t)M, (uint64_t)K, BM);
     if (rc) return rc;
     rc = get_map(m, &tb, B, (uint64_t)N, (uint64_t)K, BN);
     if (rc) return rc;
     const size_t smem = gemm_smem<BN>();
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(umma_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-        attr_set = true;
+    // the shared-memory opt-in is a per-device function attribute
+    static bool attr_set[64] = {};
+    if (m->device >= 64 || !attr_set[m->device]) {
+        cudaError_t ae = cudaFuncSetAttribute(umma_gemm_kernel<BN>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (ae != cudaSuccess) return mlp_err(m, ISMC_ERR_CUDA, "gemm smem attribute", ae);
+        if (m->device < 64) attr_set[m->device] = true;
     }
-    dim3 grid(M / BM, N / BN, splits);
-    umma_gemm_kernel<BN><<<grid, 128, smem, m->stream>>>(ta, tb, K / BK / splits, e, m->d_err);
-    cudaError_t err = cudaGetLastError();
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(M / BM, N / BN, splits);
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = m->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t err = cudaLaunchKernelEx(&cfg, umma_gemm_kernel<BN>, ta, tb, K / BK / splits, e, m->d_err);
+    if (err == cudaSuccess) err = cudaGetLastError();
     return err == cudaSuccess ? 0 : mlp_err(m, ISMC_ERR_CUDA, "gemm launch", err);
 }
 
@@ -518,6 +606,8 @@ extern "C" int ismc_mlp_create(int device, uint32_t max_batch, uint64_t seed, is
         cudaMemsetAsync(m->WTb[l], 0, (size_t)kWTRows[l] * kWTK[l] * 2, m->stream);
     }
     cudaMemsetAsync(m->dOT, 0, 128 * B * 2, m->stream);
+    cudaMemsetAsync(m->X0, 0, B * 64 * 2, m->stream);
+    cudaMemsetAsync(m->dO, 0, B * 64 * 2, m->stream);
     cudaMemsetAsync(m->d_m, 0, off * 4, m->stream);
     cudaMemsetAsync(m->d_v, 0, off * 4, m->stream);
     cudaMemsetAsync(m->d_err, 0, sizeof(int), m->stream);
@@ -579,7 +669,7 @@ static int forward(ismc_mlp* m, const float* d_x, int B) {
         e.bias = m->d_w + m->off_b[l];
         e.out_row = m->H[l]; e.ldr = 256;
         e.out_col = m->HT[l]; e.ldc = B;
-        e.out_aux = m->G[l]; e.lda = 256;
+        e.out_aux = m->G[l]; e.lda = B;
         int rc = launch_gemm<kHidBN>(m, in, B, K, m->Wb[l], 256, e);
         if (rc) return rc;
         in = m->H[l];
@@ -598,24 +688,25 @@ static int backward(ismc_mlp* m, const float* d_y, int B) {
     MCK(cudaMemsetAsync(m->d_g, 0, m->nparam * 4, m->stream));
     nll_loss_grad<<<(B + 255) / 256, 256, 0, m->stream>>>(m->O, d_y, B, 1.0f / B,
                                                           kVarFloor * kVarFloor, m->dO, m->dOT,
-                                                          m->d_loss);
+                                                          m->d_loss, m->d_g + m->off_b[3]);
     MCK(cudaGetLastError());
     const int splits = B >= 2048 ? 16 : (B >= 512 ? 4 : 1);
-    // output layer: dW4 [6 x 256] = dO^T H3, db4, dZ3 = (dO W4) * G3
+    // output layer: dW4 [6 x 256] = dO^T H3 (db4 came with the loss), dZ3 = (dO W4) * G3
+    // with db3 as its column sums
     {
         Epi e{};
         e.mode = EPI_ACC; e.M = 6; e.N = 256; e.out_f = m->d_g + m->off_w[3]; e.ldf = 256;
         int rc = launch_gemm<kHidBN>(m, m->dOT, 128, B, m->HT[2], 256, e, splits);
         if (rc) return rc;
-        bias_grad<<<6, 256, 0, m->stream>>>(m->dOT, B, 6, m->d_g + m->off_b[3]);
         Epi d{};
-        d.mode = EPI_BWD; d.M = B; d.N = 256; d.gate = m->G[2]; d.ldg = 256;
+        d.mode = EPI_BWD; d.M = B; d.N = 256; d.gate = m->G[2]; d.ldg = B;
+        d.bias_grad = m->d_g + m->off_b[2];
         d.out_row = m->dZ[2]; d.ldr = 256; d.out_col = m->dZT[2]; d.ldc = B;
         rc = launch_gemm<kHidBN>(m, m->dO, B, 64, m->WTb[3], 256, d);
         if (rc) return rc;
     }
     for (int l = 2; l >= 0; --l) {
-        // dW_l [256 x in] = dZ_l^T X_{l}, db_l
+        // dW_l [256 x in] = dZ_l^T X_{l} (db_l came with dZ_l)
         const __nv_bfloat16* XT = l ? m->HT[l - 1] : m->X0T;
         const int Kin = l ? 256 : 64;
         Epi e{};
@@ -624,11 +715,11 @@ static int backward(ismc_mlp* m, const float* d_y, int B) {
         int rc = Kin == 256 ? launch_gemm<kHidBN>(m, m->dZT[l], 256, B, XT, 256, e, splits)
                             : launch_gemm<64>(m, m->dZT[l], 256, B, XT, 64, e, splits);
         if (rc) return rc;
-        bias_grad<<<256, 256, 0, m->stream>>>(m->dZT[l], B, 256, m->d_g + m->off_b[l]);
         if (l == 0) break;
-        // dZ_{l-1} = (dZ_l W_l) * G_{l-1}
+        // dZ_{l-1} = (dZ_l W_l) * G_{l-1}, and db_{l-1} as its column sums
         Epi d{};
-        d.mode = EPI_BWD; d.M = B; d.N = 256; d.gate = m->G[l - 1]; d.ldg = 256;
+        d.mode = EPI_BWD; d.M = B; d.N = 256; d.gate = m->G[l - 1]; d.ldg = B;
+        d.bias_grad = m->d_g + m->off_b[l - 1];
         d.out_row = m->dZ[l - 1]; d.ldr = 256; d.out_col = m->dZT[l - 1]; d.ldc = B;
         rc = launch_gemm<kHidBN>(m, m->dZ[l], B, 256, m->WTb[l], 256, d);
         if (rc) return rc;
@@ -681,15 +772,16 @@ extern "C" int ismc_mlp_train_step(ismc_mlp* m, const float* d_x, const float* d
     ++m->adam_t;
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     const float bc1 = 1.0f - powf(b1, (float)m->adam_t), bc2 = 1.0f - powf(b2, (float)m->adam_t);
+    AdamSegs S{};
     for (int l = 0; l < 4; ++l) {
-        const int R = kOut[l], C = kIn[l];
-        adam_update<<<(R * C + 255) / 256, 256, 0, m->stream>>>(
-            m->d_w + m->off_w[l], m->d_g + m->off_w[l], m->d_m + m->off_w[l], m->d_v + m->off_w[l],
-            R, C, lr, b1, b2, eps, bc1, bc2, m->Wb[l], kKPad[l], l == 0 ? 5 : 0, m->WTb[l], kWTK[l]);
-        adam_update<<<(R + 255) / 256, 256, 0, m->stream>>>(
-            m->d_w + m->off_b[l], m->d_g + m->off_b[l], m->d_m + m->off_b[l], m->d_v + m->off_b[l],
-            R, 1, lr, b1, b2, eps, bc1, bc2, nullptr, 0, 0, nullptr, 0);
+        S.s[2 * l] = AdamSeg{(int)m->off_w[l], kOut[l], kIn[l], kKPad[l], l == 0 ? 5 : 0, kWTK[l],
+                             m->Wb[l], m->WTb[l]};
+        S.s[2 * l + 1] = AdamSeg{(int)m->off_b[l], kOut[l], 1, 0, 0, 0, nullptr, nullptr};
     }
+    S.n = 8;
+    const int total = (int)m->nparam;
+    adam_update<<<(total + 255) / 256, 256, 0, m->stream>>>(m->d_w, m->d_g, m->d_m, m->d_v, total, S,
+                                                           lr, b1, b2, eps, bc1, bc2);
     MCK(cudaGetLastError());
     if (loss) {
         MCK(cudaMemcpyAsync(loss, m->d_loss, 4, cudaMemcpyDeviceToHost, m->stream));

@@ -42,6 +42,18 @@ __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// ---------------------------------------------------------------- programmatic dependent launch
+// Wait until the grids this one depends on have completed and their writes are
+// visible (a no-op when the launch did not allow early start).
+__device__ __forceinline__ void grid_dep_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+// Let the next grid in the stream start its prologue; it still waits for this
+// grid's completion in grid_dep_wait before touching memory.
+__device__ __forceinline__ void grid_dep_launch() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ---------------------------------------------------------------- TMA
 // 2-D tiled load of box at (x = innermost coordinate, y) into shared memory,
 // completing on mbarrier `bar` (transaction bytes).
