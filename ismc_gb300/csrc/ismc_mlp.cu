@@ -41,6 +41,10 @@ namespace {
 constexpr int BM = 128;           // rows per tile (tcgen05 M)
 constexpr int BK = 64;            // K per stage: 64 bf16 = one 128-byte swizzle row
 constexpr uint32_t WAIT_LIMIT = 1u << 22;   // polls of a bounded try_wait: seconds at most
+// threads of a GEMM CTA: warp 0 allocates TMEM and thread 0 drives TMA and the
+// MMAs; in the epilogue warps w and w + 4 read TMEM lanes 32 (w % 4) .. + 31,
+// each for half of the tile's columns
+constexpr int GEMM_THREADS = 256;
 
 enum { EPI_HIDDEN = 0, EPI_BWD = 1, EPI_OUT = 2, EPI_ACC = 3 };
 
@@ -65,11 +69,17 @@ struct Epi {
 // 1 / (1 + e^-z); the fast divide returns 0 once e^-z passes 2^126, the limit anyway
 __device__ __forceinline__ float sigmoidf_(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 
+// K-chunk stages in flight: all four chunks of a 256-deep product for the
+// narrow tiles, two for the 256-wide tile (shared memory)
 template <int BN>
-__global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ CUtensorMap tA,
-                                                        const __grid_constant__ CUtensorMap tB,
-                                                        int k_chunks, Epi e, int* err) {
+__host__ __device__ constexpr int gemm_stages() { return BN <= 64 ? 4 : 2; }
+
+template <int BN>
+__global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_constant__ CUtensorMap tA,
+                                                                 const __grid_constant__ CUtensorMap tB,
+                                                                 int k_chunks, Epi e, int* err) {
     static_assert(BN >= 16 && BN <= 256 && BN % 16 == 0, "tile N");
+    constexpr int S = gemm_stages<BN>();
     constexpr uint32_t A_BYTES = BM * BK * 2;
     constexpr uint32_t B_BYTES = BN * BK * 2;
     constexpr uint32_t STAGE = A_BYTES + B_BYTES;
@@ -79,8 +89,8 @@ __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ 
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * STAGE);   // full[2], done[2], fin
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 5);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * STAGE);   // full[S], done[S], fin
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * S + 1);
     int* sfail = reinterpret_cast<int*>(tslot + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
@@ -91,7 +101,7 @@ __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ 
         umma::tmem_relinquish();
     }
     if (threadIdx.x == 32) {
-        for (int i = 0; i < 5; ++i) umma::mbar_init(umma::smem_u32(bars + i), 1);
+        for (int i = 0; i < 2 * S + 1; ++i) umma::mbar_init(umma::smem_u32(bars + i), 1);
         *sfail = 0;
         umma::fence_barrier_init();
     }
@@ -112,17 +122,12 @@ __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ 
             umma::tma_load_2d(sb0 + s * STAGE, &tB, (kc0 + kc) * BK, n0, bar);
         };
         bool ok = true;
-        load(0, 0);
+        // chunk j lives in stage j % S and is that stage's (j / S)-th fill;
+        // the first S chunks are requested at once
+        for (int kc = 0; kc < S && kc < k_chunks; ++kc) load(kc, kc);
         for (int kc = 0; kc < k_chunks && ok; ++kc) {
-            const int s = kc & 1;
-            if (kc + 1 < k_chunks) {
-                const int s1 = (kc + 1) & 1;
-                // stage s1 was read by the MMAs of chunk kc-1
-                if (kc >= 1 && !umma::mbar_wait(umma::smem_u32(bars + 2 + s1), ((kc - 1) >> 1) & 1,
-                                                 WAIT_LIMIT)) { ok = false; break; }
-                load(kc + 1, s1);
-            }
-            if (!umma::mbar_wait(umma::smem_u32(bars + s), (kc >> 1) & 1, WAIT_LIMIT)) {
+            const int s = kc % S;
+            if (!umma::mbar_wait(umma::smem_u32(bars + s), (kc / S) & 1, WAIT_LIMIT)) {
                 ok = false;
                 break;
             }
@@ -132,14 +137,24 @@ __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ 
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk)     // 16 bf16 = 32 B per MMA: +2 in the address field
                 umma::mma_bf16(tmem, da + 2 * kk, db + 2 * kk, IDESC, (kc | kk) != 0);
-            umma::mma_commit(umma::smem_u32(bars + 2 + s));
+            umma::mma_commit(umma::smem_u32(bars + S + s));
+            // refill the stage the previous chunk used, once its MMAs are done
+            const int pk = kc - 1, nk = pk + S;
+            if (pk >= 0 && nk < k_chunks) {
+                const int ps = pk % S;
+                if (!umma::mbar_wait(umma::smem_u32(bars + S + ps), (pk / S) & 1, WAIT_LIMIT)) {
+                    ok = false;
+                    break;
+                }
+                load(nk, ps);
+            }
         }
-        if (ok) umma::mma_commit(umma::smem_u32(bars + 4));
+        if (ok) umma::mma_commit(umma::smem_u32(bars + 2 * S));
         else *sfail = 1;
     }
     __syncthreads();
     bool ok = *sfail == 0;
-    if (ok) ok = umma::mbar_wait(umma::smem_u32(bars + 4), 0, WAIT_LIMIT);
+    if (ok) ok = umma::mbar_wait(umma::smem_u32(bars + 2 * S), 0, WAIT_LIMIT);
     // one verdict for the block: the epilogue below synchronises the block
     ok = __syncthreads_and(ok) != 0;
     // the operands are consumed: the next product may start its set-up
@@ -154,21 +169,41 @@ __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ 
         // of consecutive threads fall in distinct banks.
         constexpr int CB = BN < 64 ? BN : 64;
         constexpr int SB = CB + 8, SF = CB + 4;
-        static_assert(BN % CB == 0 && BM % CB == 0, "column blocks");
         static_assert((size_t)BM * SF * 4 <= 2 * (size_t)STAGE, "staging fits the operand stages");
         __nv_bfloat16* sb = reinterpret_cast<__nv_bfloat16*>(smem);
         float* sf = reinterpret_cast<float*>(smem);
-        const int rl = warp * 32 + lane;                     // this thread's row of the tile
+        const int q4 = warp & 3, half = warp >> 2;           // TMEM lane quarter, column half
+        const int rl = q4 * 32 + lane;                       // this thread's row of the tile
         const int r = m0 + rl;
         const bool row_ok = r < e.M;
         const bool bf = e.mode == EPI_HIDDEN || e.mode == EPI_BWD;
+        // each half of the warps takes half of a block's columns (all of a
+        // 16-wide block goes to the first half)
+        constexpr int HC = CB >= 32 ? CB / 2 : CB;
+        const int c_lo = CB >= 32 ? half * HC : (half ? CB : 0);
+        const int c_hi = CB >= 32 ? c_lo + HC : CB;
+        static_assert(BN % CB == 0 && BM % CB == 0 && GEMM_THREADS % CB == 0 && HC % 16 == 0,
+                      "column blocks");
 #pragma unroll 1
         for (int cb = 0; cb < BN; cb += CB) {
 #pragma unroll 1
-            for (int c = 0; c < CB; c += 16) {
-                float v[16];
-                umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb + c), v);
+            for (int c = c_lo; c < c_hi; c += 16) {
                 const int nb = n0 + cb + c;
+                // the chunk's bias or gate values, all loaded ahead of the TMEM
+                // read and of any store (a store between loads would serialise them)
+                float pre[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int n = nb + j;
+                    pre[j] = 0.0f;
+                    if (e.mode == EPI_BWD) {
+                        if (row_ok && n < e.N) pre[j] = __bfloat162float(e.gate[(size_t)n * e.ldg + r]);
+                    } else if (e.mode != EPI_ACC) {
+                        if (n < e.N) pre[j] = e.bias[n];
+                    }
+                }
+                float v[16];
+                umma::tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(cb + c), v);
                 if (bf) {
                     __align__(16) __nv_bfloat16 o[16];
 #pragma unroll
@@ -177,14 +212,14 @@ __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ 
                         const bool ok = row_ok && n < e.N;
                         __nv_bfloat16 b = __float2bfloat16_rn(0.0f);
                         if (ok && e.mode == EPI_HIDDEN) {
-                            const float z = v[j] + e.bias[n];
+                            const float z = v[j] + pre[j];
                             const float sg = sigmoidf_(z);
                             b = __float2bfloat16_rn(z * sg);
                             e.out_col[(size_t)n * e.ldc + r] = b;
                             e.out_aux[(size_t)n * e.lda + r] =
                                 __float2bfloat16_rn(sg * (1.0f + z * (1.0f - sg)));
                         } else if (ok) {
-                            b = __float2bfloat16_rn(v[j] * __bfloat162float(e.gate[(size_t)n * e.ldg + r]));
+                            b = __float2bfloat16_rn(v[j] * pre[j]);
                             e.out_col[(size_t)n * e.ldc + r] = b;
                         }
                         o[j] = b;
@@ -195,8 +230,7 @@ __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ 
                 } else {
                     if (e.mode == EPI_OUT) {
 #pragma unroll
-                        for (int j = 0; j < 16; ++j)
-                            if (nb + j < e.N) v[j] += e.bias[nb + j];
+                        for (int j = 0; j < 16; ++j) v[j] += pre[j];
                     }
                     float4* dst = reinterpret_cast<float4*>(sf + rl * SF + c);
 #pragma unroll
@@ -217,7 +251,7 @@ __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ 
                 }
                 if (e.mode == EPI_BWD && e.bias_grad) {
                     // column sums of the rounded dz over the tile's rows (rows past M are 0)
-                    constexpr int PARTS = 128 / CB, RPP = BM / PARTS;
+                    constexpr int PARTS = GEMM_THREADS / CB, RPP = BM / PARTS;
                     const int col = threadIdx.x % CB, part = threadIdx.x / CB;
                     if (threadIdx.x < CB * PARTS && n0 + cb + col < e.N) {
                         float acc = 0.0f;
@@ -247,7 +281,8 @@ __global__ void __launch_bounds__(128) umma_gemm_kernel(const __grid_constant__ 
 
 template <int BN>
 constexpr size_t gemm_smem() {
-    return 1024 + 2 * (size_t)(BM * BK * 2 + BN * BK * 2) + 5 * 8 + 16;
+    return 1024 + gemm_stages<BN>() * (size_t)(BM * BK * 2 + BN * BK * 2) +
+           (2 * gemm_stages<BN>() + 1) * 8 + 16;
 }
 
 // --------------------------------------------------------------------------
@@ -265,8 +300,11 @@ struct Norm { float lo[5], hi[5]; };
 // as two 16-byte vectors); rows 10-63 of X0T only ever meet gradient columns
 // that are not kept.
 __global__ void prep_inputs(const float* __restrict__ x, int B, Norm nm, __nv_bfloat16* X0,
-                            __nv_bfloat16* X0T) {
+                            __nv_bfloat16* X0T, float* loss) {
+    umma::grid_dep_wait();
+    umma::grid_dep_launch();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0) *loss = 0.0f;      // the step's loss accumulates from here (nll_loss_grad)
     if (r >= B) return;
     __align__(16) __nv_bfloat16 o[16];
 #pragma unroll
@@ -298,6 +336,8 @@ __global__ void prep_inputs(const float* __restrict__ x, int B, Norm nm, __nv_bf
 __global__ void nll_loss_grad(const float* __restrict__ O, const float* __restrict__ y, int B,
                               float inv_b, float floor2, __nv_bfloat16* dO, __nv_bfloat16* dOT,
                               float* loss, float* db) {
+    umma::grid_dep_wait();
+    umma::grid_dep_launch();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     float part[7] = {0, 0, 0, 0, 0, 0, 0};      // loss, then the six bias-gradient columns
     if (r < B) {
@@ -355,12 +395,16 @@ struct AdamSeg {
 struct AdamSegs { AdamSeg s[8]; int n; };
 
 // One Adam step of every parameter (fp32 master w, gradient g, moments m, v),
-// one thread per parameter, refreshing the bf16 copies.
-__global__ void adam_update(float* w, const float* g, float* m, float* v, int total, AdamSegs S,
+// one thread per parameter, refreshing the bf16 copies.  The gradient is
+// cleared once used: the next step's products accumulate into zeros.
+__global__ void adam_update(float* w, float* g, float* m, float* v, int total, AdamSegs S,
                             float lr, float b1, float b2, float eps, float bc1, float bc2) {
+    umma::grid_dep_wait();
+    umma::grid_dep_launch();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= total) return;
     const float gi = g[i];
+    g[i] = 0.0f;
     const float mi = b1 * m[i] + (1.0f - b1) * gi;
     const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
     m[i] = mi;
@@ -488,6 +532,24 @@ static int get_map(ismc_mlp* m, CUtensorMap* out, const void* base, uint64_t row
     return 0;
 }
 
+// Launch with programmatic stream serialisation: the kernel may start while its
+// predecessor finishes, and waits in umma::grid_dep_wait before reading memory.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
+                              Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+    return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
 template <int BN>
 static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, int N,
                        const Epi& e, int splits = 1) {
@@ -513,7 +575,7 @@ static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, 
     }
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(M / BM, N / BN, splits);
-    cfg.blockDim = dim3(128);
+    cfg.blockDim = dim3(GEMM_THREADS);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = m->stream;
     cudaLaunchAttribute attr[1];
@@ -608,6 +670,7 @@ extern "C" int ismc_mlp_create(int device, uint32_t max_batch, uint64_t seed, is
     cudaMemsetAsync(m->dOT, 0, 128 * B * 2, m->stream);
     cudaMemsetAsync(m->X0, 0, B * 64 * 2, m->stream);
     cudaMemsetAsync(m->dO, 0, B * 64 * 2, m->stream);
+    cudaMemsetAsync(m->d_g, 0, off * 4, m->stream);
     cudaMemsetAsync(m->d_m, 0, off * 4, m->stream);
     cudaMemsetAsync(m->d_v, 0, off * 4, m->stream);
     cudaMemsetAsync(m->d_err, 0, sizeof(int), m->stream);
@@ -659,8 +722,8 @@ extern "C" int ismc_mlp_set_params(ismc_mlp* m, const float* host, size_t n) {
 
 // forward pass of B rows of raw inputs; leaves H, G and O in the workspace
 static int forward(ismc_mlp* m, const float* d_x, int B) {
-    prep_inputs<<<(B + 127) / 128, 128, 0, m->stream>>>(d_x, B, g_norm, m->X0, m->X0T);
-    MCK(cudaGetLastError());
+    MCK(launch_pdl(prep_inputs, dim3((B + 127) / 128), dim3(128), m->stream, d_x, B, g_norm, m->X0,
+                   m->X0T, m->d_loss));
     const __nv_bfloat16* in = m->X0;
     int K = 64;
     for (int l = 0; l < 3; ++l) {
@@ -682,14 +745,13 @@ static int forward(ismc_mlp* m, const float* d_x, int B) {
     return launch_gemm<16>(m, in, B, 256, m->Wb[3], 16, e);
 }
 
-// gradients of the mean loss into m->d_g (and the loss into m->d_loss)
+// gradients of the mean loss added into m->d_g, which holds zeros on entry (it
+// is cleared at creation, by each Adam step and after ismc_mlp_grad), and the
+// loss into m->d_loss (cleared by prep_inputs)
 static int backward(ismc_mlp* m, const float* d_y, int B) {
-    MCK(cudaMemsetAsync(m->d_loss, 0, sizeof(float), m->stream));
-    MCK(cudaMemsetAsync(m->d_g, 0, m->nparam * 4, m->stream));
-    nll_loss_grad<<<(B + 255) / 256, 256, 0, m->stream>>>(m->O, d_y, B, 1.0f / B,
-                                                          kVarFloor * kVarFloor, m->dO, m->dOT,
-                                                          m->d_loss, m->d_g + m->off_b[3]);
-    MCK(cudaGetLastError());
+    MCK(launch_pdl(nll_loss_grad, dim3((B + 255) / 256), dim3(256), m->stream, (const float*)m->O,
+                   d_y, B, 1.0f / B, kVarFloor * kVarFloor, m->dO, m->dOT, m->d_loss,
+                   m->d_g + m->off_b[3]));
     const int splits = B >= 2048 ? 16 : (B >= 512 ? 4 : 1);
     // output layer: dW4 [6 x 256] = dO^T H3 (db4 came with the loss), dZ3 = (dO W4) * G3
     // with db3 as its column sums
@@ -757,6 +819,8 @@ extern "C" int ismc_mlp_grad(ismc_mlp* m, const float* d_x, const float* d_y, ui
     if (rc) return rc;
     if (d_grad) MCK(cudaMemcpyAsync(d_grad, m->d_g, m->nparam * 4, cudaMemcpyDeviceToDevice, m->stream));
     if (loss) MCK(cudaMemcpyAsync(loss, m->d_loss, 4, cudaMemcpyDeviceToHost, m->stream));
+    // leave the accumulator cleared for the next backward pass
+    MCK(cudaMemsetAsync(m->d_g, 0, m->nparam * 4, m->stream));
     return check_err(m);
 }
 
@@ -780,8 +844,8 @@ extern "C" int ismc_mlp_train_step(ismc_mlp* m, const float* d_x, const float* d
     }
     S.n = 8;
     const int total = (int)m->nparam;
-    adam_update<<<(total + 255) / 256, 256, 0, m->stream>>>(m->d_w, m->d_g, m->d_m, m->d_v, total, S,
-                                                           lr, b1, b2, eps, bc1, bc2);
+    MCK(launch_pdl(adam_update, dim3((total + 255) / 256), dim3(256), m->stream, m->d_w, m->d_g,
+                   m->d_m, m->d_v, total, S, lr, b1, b2, eps, bc1, bc2));
     MCK(cudaGetLastError());
     if (loss) {
         MCK(cudaMemcpyAsync(loss, m->d_loss, 4, cudaMemcpyDeviceToHost, m->stream));

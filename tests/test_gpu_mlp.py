@@ -25,7 +25,10 @@ def sur():
 
 @pytest.mark.parametrize("M,N,K,splits", [(128, 256, 64, 1), (256, 256, 256, 1), (512, 16, 256, 1),
                                           (256, 64, 4096, 16), (128, 256, 4096, 16),
-                                          (4096, 256, 256, 1)])
+                                          (4096, 256, 256, 1),
+                                          # deep K: stages refilled while the MMAs run
+                                          (256, 64, 1024, 1), (512, 16, 1280, 1),
+                                          (128, 256, 1024, 2)])
 def test_umma_gemm_matches_fp64(sur, M, N, K, splits):
     import torch
     g = torch.Generator().manual_seed(M * 7 + N + K)
