@@ -100,6 +100,10 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
         umma::tmem_alloc(umma::smem_u32(tslot), TCOLS);
         umma::tmem_relinquish();
     }
+    if (threadIdx.x == 64) {
+        umma::prefetch_tensormap(&tA);
+        umma::prefetch_tensormap(&tB);
+    }
     if (threadIdx.x == 32) {
         for (int i = 0; i < 2 * S + 1; ++i) umma::mbar_init(umma::smem_u32(bars + i), 1);
         *sfail = 0;
@@ -386,41 +390,72 @@ __global__ void nll_loss_grad(const float* __restrict__ O, const float* __restri
 // has R x C fp32 entries from `off`, and optional bf16 copies used by the
 // GEMMs: W [R x ldw] (row, K-major for the forward; with dup > 0 also at
 // column c + dup, for the first layer's split inputs) and WT [C x ldt]
-// (transposed, K-major for the backward).
+// (transposed, K-major for the backward).  A tensor is updated in 32 x 32
+// tiles, tiles_c of them across, numbered from tile0.
 struct AdamSeg {
-    int off, R, C, ldw, dup, ldt;
+    int off, R, C, ldw, dup, ldt, tile0, tiles_c;
     __nv_bfloat16* W;
     __nv_bfloat16* WT;
 };
 struct AdamSegs { AdamSeg s[8]; int n; };
 
 // One Adam step of every parameter (fp32 master w, gradient g, moments m, v),
-// one thread per parameter, refreshing the bf16 copies.  The gradient is
+// one 32 x 32 tile per block of 256 threads, refreshing the bf16 copies: the
+// row-major copy straight from the update, the transposed one through shared
+// memory so that both are written along contiguous rows.  The gradient is
 // cleared once used: the next step's products accumulate into zeros.
-__global__ void adam_update(float* w, float* g, float* m, float* v, int total, AdamSegs S,
-                            float lr, float b1, float b2, float eps, float bc1, float bc2) {
+__global__ void __launch_bounds__(256) adam_update(float* __restrict__ w, float* __restrict__ g,
+                                                   float* __restrict__ m, float* __restrict__ v,
+                                                   AdamSegs S, float lr, float b1, float b2,
+                                                   float eps, float bc1, float bc2) {
     umma::grid_dep_wait();
     umma::grid_dep_launch();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= total) return;
-    const float gi = g[i];
-    g[i] = 0.0f;
-    const float mi = b1 * m[i] + (1.0f - b1) * gi;
-    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
-    m[i] = mi;
-    v[i] = vi;
-    const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
-    w[i] = wi;
-    int k = 0;
-    while (k + 1 < S.n && i >= S.s[k + 1].off) ++k;
+    __shared__ __nv_bfloat16 tile[32][34];           // [column][row] of the tile
+    int t = blockIdx.x, k = 0;
+    while (k + 1 < S.n && t >= S.s[k + 1].tile0) ++k;
     const AdamSeg& a = S.s[k];
-    const int j = i - a.off, r = j / a.C, c = j % a.C;
-    const __nv_bfloat16 b = __float2bfloat16_rn(wi);
-    if (a.W) {
-        a.W[(size_t)r * a.ldw + c] = b;
-        if (a.dup) a.W[(size_t)r * a.ldw + c + a.dup] = b;
+    t -= a.tile0;
+    const int tr = t / a.tiles_c, tc = t % a.tiles_c;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int c = tc * 32 + tx;
+    // all four elements' operands are loaded before anything is stored
+    float gq[4], mq[4], vq[4], wq[4];
+    size_t iq[4];
+    bool okq[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int r = tr * 32 + ty + 8 * q;
+        okq[q] = r < a.R && c < a.C;
+        iq[q] = (size_t)a.off + (size_t)r * a.C + c;
+        if (okq[q]) { gq[q] = g[iq[q]]; mq[q] = m[iq[q]]; vq[q] = v[iq[q]]; wq[q] = w[iq[q]]; }
     }
-    if (a.WT) a.WT[(size_t)c * a.ldt + r] = b;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (!okq[q]) continue;
+        const int rr = ty + 8 * q, r = tr * 32 + rr;
+        const float gi = gq[q];
+        const float mi = b1 * mq[q] + (1.0f - b1) * gi;
+        const float vi = b2 * vq[q] + (1.0f - b2) * gi * gi;
+        const float wi = wq[q] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+        g[iq[q]] = 0.0f;
+        m[iq[q]] = mi;
+        v[iq[q]] = vi;
+        w[iq[q]] = wi;
+        const __nv_bfloat16 b = __float2bfloat16_rn(wi);
+        if (a.W) {
+            a.W[(size_t)r * a.ldw + c] = b;
+            if (a.dup) a.W[(size_t)r * a.ldw + c + a.dup] = b;
+        }
+        tile[tx][rr] = b;
+    }
+    if (a.WT) {                                      // the same for the whole block
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int cc = ty + 8 * q, c2 = tc * 32 + cc, r2 = tr * 32 + tx;
+            if (c2 < a.C && r2 < a.R) a.WT[(size_t)c2 * a.ldt + r2] = tile[cc][tx];
+        }
+    }
 }
 
 // bf16 copies of a parameter tensor without an update
@@ -837,15 +872,20 @@ extern "C" int ismc_mlp_train_step(ismc_mlp* m, const float* d_x, const float* d
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     const float bc1 = 1.0f - powf(b1, (float)m->adam_t), bc2 = 1.0f - powf(b2, (float)m->adam_t);
     AdamSegs S{};
+    int tiles = 0;
     for (int l = 0; l < 4; ++l) {
-        S.s[2 * l] = AdamSeg{(int)m->off_w[l], kOut[l], kIn[l], kKPad[l], l == 0 ? 5 : 0, kWTK[l],
-                             m->Wb[l], m->WTb[l]};
-        S.s[2 * l + 1] = AdamSeg{(int)m->off_b[l], kOut[l], 1, 0, 0, 0, nullptr, nullptr};
+        for (int h = 0; h < 2; ++h) {
+            const int R = kOut[l], C = h ? 1 : kIn[l];
+            const int tc = (C + 31) / 32, tr = (R + 31) / 32;
+            S.s[2 * l + h] = h ? AdamSeg{(int)m->off_b[l], R, 1, 0, 0, 0, tiles, tc, nullptr, nullptr}
+                               : AdamSeg{(int)m->off_w[l], R, C, kKPad[l], l == 0 ? 5 : 0, kWTK[l],
+                                         tiles, tc, m->Wb[l], m->WTb[l]};
+            tiles += tr * tc;
+        }
     }
     S.n = 8;
-    const int total = (int)m->nparam;
-    MCK(launch_pdl(adam_update, dim3((total + 255) / 256), dim3(256), m->stream, m->d_w, m->d_g,
-                   m->d_m, m->d_v, total, S, lr, b1, b2, eps, bc1, bc2));
+    MCK(launch_pdl(adam_update, dim3(tiles), dim3(256), m->stream, m->d_w, m->d_g, m->d_m, m->d_v,
+                   S, lr, b1, b2, eps, bc1, bc2));
     MCK(cudaGetLastError());
     if (loss) {
         MCK(cudaMemcpyAsync(loss, m->d_loss, 4, cudaMemcpyDeviceToHost, m->stream));

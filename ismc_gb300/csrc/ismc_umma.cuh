@@ -55,6 +55,11 @@ __device__ __forceinline__ void grid_dep_launch() {
 }
 
 // ---------------------------------------------------------------- TMA
+// Bring a tensor map (a kernel parameter) into the TMA unit's descriptor cache
+// ahead of its first use.
+__device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
 // 2-D tiled load of box at (x = innermost coordinate, y) into shared memory,
 // completing on mbarrier `bar` (transaction bytes).
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
