@@ -264,6 +264,16 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
                         atomicAdd(e.bias_grad + n0 + cb + col, acc);
                     }
                 }
+            } else if (e.mode == EPI_ACC && !e.fold && e.ldf % 4 == 0 && e.N % 4 == 0) {
+                // split-K partial sums as 16-byte vector atomics along rows
+                constexpr int QPR = CB / 4;
+                for (int idx = threadIdx.x; idx < BM * QPR; idx += blockDim.x) {
+                    const int row = idx / QPR, col = (idx % QPR) * 4;
+                    const int gr = m0 + row, gn = n0 + cb + col;
+                    if (gr < e.M && gn < e.N)
+                        atomicAdd(reinterpret_cast<float4*>(e.out_f + (size_t)gr * e.ldf + gn),
+                                  *reinterpret_cast<const float4*>(sf + row * SF + col));
+                }
             } else {
                 for (int idx = threadIdx.x; idx < BM * CB; idx += blockDim.x) {
                     const int row = idx / CB, col = idx % CB;
