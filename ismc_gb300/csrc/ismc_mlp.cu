@@ -74,7 +74,7 @@ __device__ __forceinline__ float sigmoidf_(float z) { return __fdividef(1.0f, 1.
 template <int BN>
 __host__ __device__ constexpr int gemm_stages() { return BN <= 64 ? 4 : 2; }
 
-template <int BN>
+template <int BN, int MODE>
 __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_constant__ CUtensorMap tA,
                                                                  const __grid_constant__ CUtensorMap tB,
                                                                  int k_chunks, Epi e, int* err) {
@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
         const int rl = q4 * 32 + lane;                       // this thread's row of the tile
         const int r = m0 + rl;
         const bool row_ok = r < e.M;
-        const bool bf = e.mode == EPI_HIDDEN || e.mode == EPI_BWD;
+        constexpr bool bf = MODE == EPI_HIDDEN || MODE == EPI_BWD;
         // each half of the warps takes half of a block's columns (all of a
         // 16-wide block goes to the first half)
         constexpr int HC = CB >= 32 ? CB / 2 : CB;
@@ -200,22 +200,22 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
                 for (int j = 0; j < 16; ++j) {
                     const int n = nb + j;
                     pre[j] = 0.0f;
-                    if (e.mode == EPI_BWD) {
+                    if constexpr (MODE == EPI_BWD) {
                         if (row_ok && n < e.N) pre[j] = __bfloat162float(e.gate[(size_t)n * e.ldg + r]);
-                    } else if (e.mode != EPI_ACC) {
+                    } else if constexpr (MODE != EPI_ACC) {
                         if (n < e.N) pre[j] = e.bias[n];
                     }
                 }
                 float v[16];
                 umma::tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(cb + c), v);
-                if (bf) {
+                if constexpr (bf) {
                     __align__(16) __nv_bfloat16 o[16];
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         const int n = nb + j;
                         const bool ok = row_ok && n < e.N;
                         __nv_bfloat16 b = __float2bfloat16_rn(0.0f);
-                        if (ok && e.mode == EPI_HIDDEN) {
+                        if (ok && MODE == EPI_HIDDEN) {
                             const float z = v[j] + pre[j];
                             const float sg = sigmoidf_(z);
                             b = __float2bfloat16_rn(z * sg);
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
                     dst[0] = reinterpret_cast<const uint4*>(o)[0];
                     dst[1] = reinterpret_cast<const uint4*>(o)[1];
                 } else {
-                    if (e.mode == EPI_OUT) {
+                    if constexpr (MODE == EPI_OUT) {
 #pragma unroll
                         for (int j = 0; j < 16; ++j) v[j] += pre[j];
                     }
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
                 }
             }
             __syncthreads();
-            if (bf) {
+            if constexpr (bf) {
                 // row-major copy: CB / 8 16-byte vectors per row (N is a multiple of CB here)
                 constexpr int VPR = CB / 8;
                 for (int idx = threadIdx.x; idx < BM * VPR; idx += blockDim.x) {
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
                         *reinterpret_cast<uint4*>(e.out_row + (size_t)gr * e.ldr + gn) =
                             *reinterpret_cast<const uint4*>(sb + row * SB + q * 8);
                 }
-                if (e.mode == EPI_BWD && e.bias_grad) {
+                if (MODE == EPI_BWD && e.bias_grad) {
                     // column sums of the rounded dz over the tile's rows (rows past M are 0)
                     constexpr int PARTS = GEMM_THREADS / CB, RPP = BM / PARTS;
                     const int col = threadIdx.x % CB, part = threadIdx.x / CB;
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
                         atomicAdd(e.bias_grad + n0 + cb + col, acc);
                     }
                 }
-            } else if (e.mode == EPI_ACC && !e.fold && e.ldf % 4 == 0 && e.N % 4 == 0) {
+            } else if (MODE == EPI_ACC && !e.fold && e.ldf % 4 == 0 && e.N % 4 == 0) {
                 // split-K partial sums as 16-byte vector atomics along rows
                 constexpr int QPR = CB / 4;
                 for (int idx = threadIdx.x; idx < BM * QPR; idx += blockDim.x) {
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
                     const int gr = m0 + row, gn = n0 + cb + col;
                     if (gr < e.M && gn < e.N) {
                         const float x = sf[row * SF + col];
-                        if (e.mode == EPI_OUT) e.out_f[(size_t)gr * e.ldf + gn] = x;
+                        if (MODE == EPI_OUT) e.out_f[(size_t)gr * e.ldf + gn] = x;
                         else atomicAdd(e.out_f + (size_t)gr * e.ldf + (e.fold ? gn % e.fold : gn), x);
                     }
                 }
@@ -595,14 +595,17 @@ static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, c
     return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
-template <int BN>
+// One product with the epilogue MODE (a template argument of the kernel, so
+// that each epilogue compiles without the others' branches; e.mode must match).
+template <int BN, int MODE>
 static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, int N,
                        const Epi& e, int splits = 1) {
     // A: [M x K] bf16, B: [N x K] bf16, both K-major; M % 128 == 0, N % BN == 0, K % 64 == 0
+    if (e.mode != MODE) return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: epilogue mode mismatch");
     if (M % BM || N % BN || K % (BK * splits))
         return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: shape not tileable");
     // bf16 row-major outputs leave as 16-byte vectors of 8 columns
-    if ((e.mode == EPI_HIDDEN || e.mode == EPI_BWD) && (e.N % 8 || e.ldr % 8))
+    if ((MODE == EPI_HIDDEN || MODE == EPI_BWD) && (e.N % 8 || e.ldr % 8))
         return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: row-major output not 16-byte tileable");
     CUtensorMap ta, tb;
     int rc = get_map(m, &ta, A, (uint64_t)M, (uint64_t)K, BM);
@@ -613,7 +616,7 @@ static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, 
     // the shared-memory opt-in is a per-device function attribute
     static bool attr_set[64] = {};
     if (m->device >= 64 || !attr_set[m->device]) {
-        cudaError_t ae = cudaFuncSetAttribute(umma_gemm_kernel<BN>,
+        cudaError_t ae = cudaFuncSetAttribute(umma_gemm_kernel<BN, MODE>,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (ae != cudaSuccess) return mlp_err(m, ISMC_ERR_CUDA, "gemm smem attribute", ae);
         if (m->device < 64) attr_set[m->device] = true;
@@ -628,7 +631,8 @@ static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, 
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t err = cudaLaunchKernelEx(&cfg, umma_gemm_kernel<BN>, ta, tb, K / BK / splits, e, m->d_err);
+    cudaError_t err = cudaLaunchKernelEx(&cfg, umma_gemm_kernel<BN, MODE>, ta, tb, K / BK / splits, e,
+                                         m->d_err);
     if (err == cudaSuccess) err = cudaGetLastError();
     return err == cudaSuccess ? 0 : mlp_err(m, ISMC_ERR_CUDA, "gemm launch", err);
 }
@@ -778,7 +782,7 @@ static int forward(ismc_mlp* m, const float* d_x, int B) {
         e.out_row = m->H[l]; e.ldr = 256;
         e.out_col = m->HT[l]; e.ldc = B;
         e.out_aux = m->G[l]; e.lda = B;
-        int rc = launch_gemm<kHidBN>(m, in, B, K, m->Wb[l], 256, e);
+        int rc = launch_gemm<kHidBN, EPI_HIDDEN>(m, in, B, K, m->Wb[l], 256, e);
         if (rc) return rc;
         in = m->H[l];
         K = 256;
@@ -787,7 +791,7 @@ static int forward(ismc_mlp* m, const float* d_x, int B) {
     e.mode = EPI_OUT; e.M = B; e.N = 6;
     e.bias = m->d_w + m->off_b[3];
     e.out_f = m->O; e.ldf = 16;
-    return launch_gemm<16>(m, in, B, 256, m->Wb[3], 16, e);
+    return launch_gemm<16, EPI_OUT>(m, in, B, 256, m->Wb[3], 16, e);
 }
 
 // gradients of the mean loss added into m->d_g, which holds zeros on entry (it
@@ -803,13 +807,13 @@ static int backward(ismc_mlp* m, const float* d_y, int B) {
     {
         Epi e{};
         e.mode = EPI_ACC; e.M = 6; e.N = 256; e.out_f = m->d_g + m->off_w[3]; e.ldf = 256;
-        int rc = launch_gemm<kHidBN>(m, m->dOT, 128, B, m->HT[2], 256, e, splits);
+        int rc = launch_gemm<kHidBN, EPI_ACC>(m, m->dOT, 128, B, m->HT[2], 256, e, splits);
         if (rc) return rc;
         Epi d{};
         d.mode = EPI_BWD; d.M = B; d.N = 256; d.gate = m->G[2]; d.ldg = B;
         d.bias_grad = m->d_g + m->off_b[2];
         d.out_row = m->dZ[2]; d.ldr = 256; d.out_col = m->dZT[2]; d.ldc = B;
-        rc = launch_gemm<kHidBN>(m, m->dO, B, 64, m->WTb[3], 256, d);
+        rc = launch_gemm<kHidBN, EPI_BWD>(m, m->dO, B, 64, m->WTb[3], 256, d);
         if (rc) return rc;
     }
     for (int l = 2; l >= 0; --l) {
@@ -819,8 +823,8 @@ static int backward(ismc_mlp* m, const float* d_y, int B) {
         Epi e{};
         e.mode = EPI_ACC; e.M = 256; e.N = kIn[l]; e.out_f = m->d_g + m->off_w[l]; e.ldf = kIn[l];
         if (l == 0) { e.N = 10; e.fold = 5; }     // hi and lo input columns share the weights
-        int rc = Kin == 256 ? launch_gemm<kHidBN>(m, m->dZT[l], 256, B, XT, 256, e, splits)
-                            : launch_gemm<64>(m, m->dZT[l], 256, B, XT, 64, e, splits);
+        int rc = Kin == 256 ? launch_gemm<kHidBN, EPI_ACC>(m, m->dZT[l], 256, B, XT, 256, e, splits)
+                            : launch_gemm<64, EPI_ACC>(m, m->dZT[l], 256, B, XT, 64, e, splits);
         if (rc) return rc;
         if (l == 0) break;
         // dZ_{l-1} = (dZ_l W_l) * G_{l-1}, and db_{l-1} as its column sums
@@ -828,7 +832,7 @@ static int backward(ismc_mlp* m, const float* d_y, int B) {
         d.mode = EPI_BWD; d.M = B; d.N = 256; d.gate = m->G[l - 1]; d.ldg = B;
         d.bias_grad = m->d_g + m->off_b[l - 1];
         d.out_row = m->dZ[l - 1]; d.ldr = 256; d.out_col = m->dZT[l - 1]; d.ldc = B;
-        rc = launch_gemm<kHidBN>(m, m->dZ[l], B, 256, m->WTb[l], 256, d);
+        rc = launch_gemm<kHidBN, EPI_BWD>(m, m->dZ[l], B, 256, m->WTb[l], 256, d);
         if (rc) return rc;
     }
     MCK(cudaGetLastError());
@@ -936,9 +940,9 @@ extern "C" int ismc_mlp_gemm_test(ismc_mlp* m, const void* A, const void* Bm, fl
     Epi e{};
     e.mode = EPI_ACC; e.M = M; e.N = N; e.out_f = D; e.ldf = N;
     int rc;
-    if (N % 256 == 0) rc = launch_gemm<256>(m, A, M, K, Bm, N, e, splits);
-    else if (N % 64 == 0) rc = launch_gemm<64>(m, A, M, K, Bm, N, e, splits);
-    else rc = launch_gemm<16>(m, A, M, K, Bm, N, e, splits);
+    if (N % 256 == 0) rc = launch_gemm<256, EPI_ACC>(m, A, M, K, Bm, N, e, splits);
+    else if (N % 64 == 0) rc = launch_gemm<64, EPI_ACC>(m, A, M, K, Bm, N, e, splits);
+    else rc = launch_gemm<16, EPI_ACC>(m, A, M, K, Bm, N, e, splits);
     if (rc) return rc;
     return check_err(m);
 }
