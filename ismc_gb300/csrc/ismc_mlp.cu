@@ -181,6 +181,8 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
         const int r = m0 + rl;
         const bool row_ok = r < e.M;
         constexpr bool bf = MODE == EPI_HIDDEN || MODE == EPI_BWD;
+        // the bf16 epilogues run on whole tiles only (checked at launch): no bounds tests
+        constexpr bool bf_full = bf;
         // each half of the warps takes half of a block's columns (all of a
         // 16-wide block goes to the first half)
         constexpr int HC = CB >= 32 ? CB / 2 : CB;
@@ -201,9 +203,10 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
                     const int n = nb + j;
                     pre[j] = 0.0f;
                     if constexpr (MODE == EPI_BWD) {
-                        if (row_ok && n < e.N) pre[j] = __bfloat162float(e.gate[(size_t)n * e.ldg + r]);
+                        if (bf_full || (row_ok && n < e.N))
+                            pre[j] = __bfloat162float(e.gate[(size_t)n * e.ldg + r]);
                     } else if constexpr (MODE != EPI_ACC) {
-                        if (n < e.N) pre[j] = e.bias[n];
+                        if (bf_full || n < e.N) pre[j] = e.bias[n];
                     }
                 }
                 float v[16];
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         const int n = nb + j;
-                        const bool ok = row_ok && n < e.N;
+                        const bool ok = bf_full || (row_ok && n < e.N);
                         __nv_bfloat16 b = __float2bfloat16_rn(0.0f);
                         if (ok && MODE == EPI_HIDDEN) {
                             const float z = v[j] + pre[j];
@@ -249,7 +252,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
                 for (int idx = threadIdx.x; idx < BM * VPR; idx += blockDim.x) {
                     const int row = idx / VPR, q = idx % VPR;
                     const int gr = m0 + row, gn = n0 + cb + q * 8;
-                    if (gr < e.M && gn < e.N)
+                    if (bf_full || (gr < e.M && gn < e.N))
                         *reinterpret_cast<uint4*>(e.out_row + (size_t)gr * e.ldr + gn) =
                             *reinterpret_cast<const uint4*>(sb + row * SB + q * 8);
                 }
@@ -257,7 +260,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
                     // column sums of the rounded dz over the tile's rows (rows past M are 0)
                     constexpr int PARTS = GEMM_THREADS / CB, RPP = BM / PARTS;
                     const int col = threadIdx.x % CB, part = threadIdx.x / CB;
-                    if (threadIdx.x < CB * PARTS && n0 + cb + col < e.N) {
+                    if (threadIdx.x < CB * PARTS && (bf_full || n0 + cb + col < e.N)) {
                         float acc = 0.0f;
                         for (int row = part * RPP; row < (part + 1) * RPP; ++row)
                             acc += __bfloat162float(sb[row * SB + col]);
@@ -604,9 +607,10 @@ static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, 
     if (e.mode != MODE) return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: epilogue mode mismatch");
     if (M % BM || N % BN || K % (BK * splits))
         return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: shape not tileable");
-    // bf16 row-major outputs leave as 16-byte vectors of 8 columns
-    if ((MODE == EPI_HIDDEN || MODE == EPI_BWD) && (e.N % 8 || e.ldr % 8))
-        return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: row-major output not 16-byte tileable");
+    // bf16 row-major outputs leave as 16-byte vectors of 8 columns, and the
+    // bf16 epilogues assume whole tiles (no bounds tests)
+    if ((MODE == EPI_HIDDEN || MODE == EPI_BWD) && (e.N % 8 || e.ldr % 8 || e.M != M || e.N != N))
+        return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: bf16 epilogue needs whole 16-byte-aligned tiles");
     CUtensorMap ta, tb;
     int rc = get_map(m, &ta, A, (uint64_t)M, (uint64_t)K, BM);
     if (rc) return rc;
