@@ -30,6 +30,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -63,7 +64,7 @@ struct Epi {
     int lda;
     float* out_f;                  // [M x ldf]
     int ldf;
-    int fold;                      // EPI_ACC: column n accumulates into n % fold (0: n)
+    int fold;                      // EPI_ACC: columns n and n + fold accumulate into n (0: none)
 };
 
 // 1 / (1 + e^-z); the fast divide returns 0 once e^-z passes 2^126, the limit anyway
@@ -75,7 +76,7 @@ template <int BN>
 __host__ __device__ constexpr int gemm_stages() { return BN <= 64 ? 4 : 2; }
 
 template <int BN, int MODE>
-__global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_constant__ CUtensorMap tA,
+__global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(const __grid_constant__ CUtensorMap tA,
                                                                  const __grid_constant__ CUtensorMap tB,
                                                                  int k_chunks, Epi e, int* err) {
     static_assert(BN >= 16 && BN <= 256 && BN % 16 == 0, "tile N");
@@ -116,6 +117,44 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
     // Launched with programmatic stream serialisation, the set-up above overlaps
     // the previous product's tail; every global access comes after this wait.
     umma::grid_dep_wait();
+
+    // Epilogue geometry.  Blocks of CB columns are staged, after the last MMA,
+    // in the operand stages: bf16 rows of SB elements (hidden / backward) or
+    // fp32 rows of SF (output / gradient), padded so that the 16-byte row
+    // writes of consecutive threads fall in distinct banks.  Warps w and w + 4
+    // read TMEM lanes 32 (w % 4) .. + 31 (one row per thread) and each take
+    // half of a block's columns (all of a 16-wide block goes to the first half).
+    constexpr int CB = BN < 64 ? BN : 64;
+    constexpr int SB = CB + 8, SF = CB + 4;
+    constexpr int HC = CB >= 32 ? CB / 2 : CB;
+    static_assert(BN % CB == 0 && BM % CB == 0 && GEMM_THREADS % CB == 0 && HC % 16 == 0,
+                  "column blocks");
+    static_assert((size_t)BM * SF * 4 <= 2 * (size_t)STAGE, "staging fits the operand stages");
+    constexpr bool bf = MODE == EPI_HIDDEN || MODE == EPI_BWD;
+    // the bf16 epilogues run on whole tiles only (checked at launch): no bounds tests
+    constexpr bool bf_full = bf;
+    // with a single column block, the bias or gate values of this thread's
+    // columns are loaded now, while the operand tiles stream in and the MMAs run
+    constexpr bool PRE = BN == CB && MODE != EPI_ACC;
+    static_assert(PRE || MODE == EPI_ACC, "bias and gate epilogues use one column block");
+    const int q4 = warp & 3, half = warp >> 2;           // TMEM lane quarter, column half
+    const int rl = q4 * 32 + lane;                       // this thread's row of the tile
+    const int r = m0 + rl;
+    const bool row_ok = r < e.M;
+    const int c_lo = CB >= 32 ? half * HC : (half ? CB : 0);
+    const int c_hi = CB >= 32 ? c_lo + HC : CB;
+    float pl[PRE ? HC : 1];
+    if constexpr (PRE) {
+#pragma unroll
+        for (int k = 0; k < HC; ++k) {
+            const int n = n0 + c_lo + k;
+            pl[k] = 0.0f;
+            if (c_lo < c_hi) {
+                if constexpr (MODE == EPI_BWD) pl[k] = __bfloat162float(e.gate[(size_t)n * e.ldg + r]);
+                else if (bf_full || n < e.N) pl[k] = e.bias[n];
+            }
+        }
+    }
 
     if (threadIdx.x == 0) {
         const uint32_t sa0 = umma::smem_u32(smem), sb0 = sa0 + A_BYTES;
@@ -167,48 +206,19 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
         if (threadIdx.x == 0) atomicExch(err, 1);
     } else {
         umma::fence_after_sync();
-        // The last MMA has read the operand stages, so blocks of CB columns are
-        // staged there: bf16 rows of SB elements (hidden / backward) or fp32
-        // rows of SF (output / gradient), padded so that the 16-byte row writes
-        // of consecutive threads fall in distinct banks.
-        constexpr int CB = BN < 64 ? BN : 64;
-        constexpr int SB = CB + 8, SF = CB + 4;
-        static_assert((size_t)BM * SF * 4 <= 2 * (size_t)STAGE, "staging fits the operand stages");
+        // the last MMA has read the operand stages: they hold the staged blocks now
         __nv_bfloat16* sb = reinterpret_cast<__nv_bfloat16*>(smem);
         float* sf = reinterpret_cast<float*>(smem);
-        const int q4 = warp & 3, half = warp >> 2;           // TMEM lane quarter, column half
-        const int rl = q4 * 32 + lane;                       // this thread's row of the tile
-        const int r = m0 + rl;
-        const bool row_ok = r < e.M;
-        constexpr bool bf = MODE == EPI_HIDDEN || MODE == EPI_BWD;
-        // the bf16 epilogues run on whole tiles only (checked at launch): no bounds tests
-        constexpr bool bf_full = bf;
-        // each half of the warps takes half of a block's columns (all of a
-        // 16-wide block goes to the first half)
-        constexpr int HC = CB >= 32 ? CB / 2 : CB;
-        const int c_lo = CB >= 32 ? half * HC : (half ? CB : 0);
-        const int c_hi = CB >= 32 ? c_lo + HC : CB;
-        static_assert(BN % CB == 0 && BM % CB == 0 && GEMM_THREADS % CB == 0 && HC % 16 == 0,
-                      "column blocks");
 #pragma unroll 1
         for (int cb = 0; cb < BN; cb += CB) {
-#pragma unroll 1
-            for (int c = c_lo; c < c_hi; c += 16) {
+#pragma unroll
+            for (int cc = 0; cc < HC; cc += 16) {
+                const int c = c_lo + cc;
+                if (c >= c_hi) break;                      // (same for the whole warp)
                 const int nb = n0 + cb + c;
-                // the chunk's bias or gate values, all loaded ahead of the TMEM
-                // read and of any store (a store between loads would serialise them)
                 float pre[16];
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int n = nb + j;
-                    pre[j] = 0.0f;
-                    if constexpr (MODE == EPI_BWD) {
-                        if (bf_full || (row_ok && n < e.N))
-                            pre[j] = __bfloat162float(e.gate[(size_t)n * e.ldg + r]);
-                    } else if constexpr (MODE != EPI_ACC) {
-                        if (bf_full || n < e.N) pre[j] = e.bias[n];
-                    }
-                }
+                for (int j = 0; j < 16; ++j) pre[j] = PRE ? pl[(PRE ? cc : 0) + j] : 0.0f;
                 float v[16];
                 umma::tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(cb + c), v);
                 if constexpr (bf) {
@@ -267,7 +277,19 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
                         atomicAdd(e.bias_grad + n0 + cb + col, acc);
                     }
                 }
-            } else if (MODE == EPI_ACC && !e.fold && e.ldf % 4 == 0 && e.N % 4 == 0) {
+            } else if (MODE == EPI_ACC && e.fold) {
+                // the input's hi and lo columns n and n + fold share a weight
+                // (one tile holds both, checked at launch): add them, then one
+                // atomic per row and weight
+                const int nf = e.fold;
+                for (int idx = threadIdx.x; idx < BM * nf; idx += blockDim.x) {
+                    const int row = idx / nf, col = idx % nf;
+                    const int gr = m0 + row;
+                    if (gr < e.M)
+                        atomicAdd(e.out_f + (size_t)gr * e.ldf + col,
+                                  sf[row * SF + col] + sf[row * SF + col + nf]);
+                }
+            } else if (MODE == EPI_ACC && e.ldf % 4 == 0 && e.N % 4 == 0) {
                 // split-K partial sums as 16-byte vector atomics along rows
                 constexpr int QPR = CB / 4;
                 for (int idx = threadIdx.x; idx < BM * QPR; idx += blockDim.x) {
@@ -284,7 +306,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) umma_gemm_kernel(const __grid_co
                     if (gr < e.M && gn < e.N) {
                         const float x = sf[row * SF + col];
                         if (MODE == EPI_OUT) e.out_f[(size_t)gr * e.ldf + gn] = x;
-                        else atomicAdd(e.out_f + (size_t)gr * e.ldf + (e.fold ? gn % e.fold : gn), x);
+                        else atomicAdd(e.out_f + (size_t)gr * e.ldf + gn, x);
                     }
                 }
             }
@@ -605,6 +627,9 @@ static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, 
                        const Epi& e, int splits = 1) {
     // A: [M x K] bf16, B: [N x K] bf16, both K-major; M % 128 == 0, N % BN == 0, K % 64 == 0
     if (e.mode != MODE) return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: epilogue mode mismatch");
+    // folded gradient columns: both halves in the first (only) block of one tile
+    if (e.fold && (MODE != EPI_ACC || N != BN || e.N != 2 * e.fold || e.N > (BN < 64 ? BN : 64)))
+        return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: folded columns must share one tile");
     if (M % BM || N % BN || K % (BK * splits))
         return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: shape not tileable");
     // bf16 row-major outputs leave as 16-byte vectors of 8 columns, and the
@@ -805,13 +830,21 @@ static int backward(ismc_mlp* m, const float* d_y, int B) {
     MCK(launch_pdl(nll_loss_grad, dim3((B + 255) / 256), dim3(256), m->stream, (const float*)m->O,
                    d_y, B, 1.0f / B, kVarFloor * kVarFloor, m->dO, m->dOT, m->d_loss,
                    m->d_g + m->off_b[3]));
-    const int splits = B >= 2048 ? 16 : (B >= 512 ? 4 : 1);
+    // split-K over the batch for the weight gradients: about 128 CTAs per
+    // product (a power of two of 64-row slices that divides the batch)
+    auto splits_for = [B](int tiles) {
+        const int want = std::max(1, 128 / tiles);
+        int sp = 1;
+        while (sp * 2 <= want && (B / BK) % (sp * 2) == 0) sp *= 2;
+        return sp;
+    };
     // output layer: dW4 [6 x 256] = dO^T H3 (db4 came with the loss), dZ3 = (dO W4) * G3
     // with db3 as its column sums
     {
         Epi e{};
         e.mode = EPI_ACC; e.M = 6; e.N = 256; e.out_f = m->d_g + m->off_w[3]; e.ldf = 256;
-        int rc = launch_gemm<kHidBN, EPI_ACC>(m, m->dOT, 128, B, m->HT[2], 256, e, splits);
+        int rc = launch_gemm<kHidBN, EPI_ACC>(m, m->dOT, 128, B, m->HT[2], 256, e,
+                                              splits_for(256 / kHidBN));
         if (rc) return rc;
         Epi d{};
         d.mode = EPI_BWD; d.M = B; d.N = 256; d.gate = m->G[2]; d.ldg = B;
@@ -827,8 +860,10 @@ static int backward(ismc_mlp* m, const float* d_y, int B) {
         Epi e{};
         e.mode = EPI_ACC; e.M = 256; e.N = kIn[l]; e.out_f = m->d_g + m->off_w[l]; e.ldf = kIn[l];
         if (l == 0) { e.N = 10; e.fold = 5; }     // hi and lo input columns share the weights
-        int rc = Kin == 256 ? launch_gemm<kHidBN, EPI_ACC>(m, m->dZT[l], 256, B, XT, 256, e, splits)
-                            : launch_gemm<64, EPI_ACC>(m, m->dZT[l], 256, B, XT, 64, e, splits);
+        int rc = Kin == 256
+                     ? launch_gemm<kHidBN, EPI_ACC>(m, m->dZT[l], 256, B, XT, 256, e,
+                                                    splits_for(2 * 256 / kHidBN))
+                     : launch_gemm<64, EPI_ACC>(m, m->dZT[l], 256, B, XT, 64, e, splits_for(2));
         if (rc) return rc;
         if (l == 0) break;
         // dZ_{l-1} = (dZ_l W_l) * G_{l-1}, and db_{l-1} as its column sums
