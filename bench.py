@@ -465,6 +465,24 @@ def run_other_workload(args):
     if args.workload == "dropin":
         run_dropin_workload()
         return
+    if args.workload == "train":
+        r = benchmarks.run_train(epochs=max(2, int(8 * s)))
+        peaks = load_measured_peaks()
+        peak = peaks.get("bf16_tflops")
+        line = {"metric": "surrogate training steps/s", "value": r["steps_per_s"],
+                "unit": "steps/s", "higher_is_better": True, "workload": "train",
+                "dtype": "bf16 (fp32 accumulate)",
+                "config": {"workload": "MLP 5-256-256-256-6, batch 4096, Gaussian NLL + Adam, "
+                                       "device-resident synthetic rows", "scale": s},
+                "roofline": {"bound": "tensor", "unit": "TFLOP/s", "achieved": r["tflops"],
+                             "peak": peak, "frac": r["tflops"] / peak if peak else None,
+                             "traffic": None,
+                             "note": "algorithmic FLOP per step over host-timed steps (14 "
+                                     "launches each); peak = measured bf16 burst "
+                                     "(MEASURED_PEAKS.json, of measured)"},
+                "result": r}
+        print(json.dumps(line), flush=True)
+        return
     if args.workload == "tables":
         r, data = benchmarks.run_tables(eng, grid=max(8, int(64 * min(1.0, s))),
                                         N=max(50, int(1000 * min(1.0, s))), M=100)
@@ -515,7 +533,7 @@ def main():
     ap.add_argument("--packets", type=int, default=PACKETS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["forward", "lookup", "tables", "surrogate", "solve",
-                                           "dropin"],
+                                           "dropin", "train"],
                     default="forward")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="size factor for the secondary workloads (1 = full benchmark size)")

@@ -9,6 +9,8 @@
              held-out error against high-count Monte Carlo)
   solve      batched inverse solve: plain path (PRAXIS on Monte Carlo) against
              the surrogate-assisted path (solves/s, error vs truth, fallbacks)
+  train      bare training steps of the MLP at batch 4096 on device-resident
+             synthetic rows (steps/s, and FLOP/s against the tensor-core peak)
 
 All inputs are synthetic and seeded; sizes scale with `scale` so the same code
 runs as a quick check or at the full sizes of the benchmark set.
@@ -87,6 +89,12 @@ def run_surrogate(engine, n_samples=1 << 20, packets=100_000, epochs=20, batch=4
     t0 = time.perf_counter()
     Y, S = simulate(engine, X, packets, seed=seed)
     t_gen = time.perf_counter() - t0
+    # first use of the shuffle and gather kernels (module loading, and any
+    # just-in-time compilation of the framework's own kernels) on a throwaway
+    # network, outside the timed training
+    warm = Surrogate(0, max_batch=batch, seed=seed)
+    warm.train(X[:batch].astype(np.float32), Y[:batch].astype(np.float32), epochs=1, batch=batch)
+    warm.close()
     sur = Surrogate(0, max_batch=batch, seed=seed)
     t1 = time.perf_counter()
     hist = sur.train(X.astype(np.float32), Y.astype(np.float32), epochs=epochs, batch=batch,
@@ -176,3 +184,50 @@ def run_solve(engine, sur, n_meas=10000, n_plain=200, seed=4, verify_packets=1_0
             "corrected_rate": float(rs["corrected"].mean()),
             "fallback_rate": float(rs["fallback"].mean()), "surrogate_timing": rs["timing"],
             "speedup": (n_meas / t_sur) / (k / t_plain)}
+
+
+# Algorithmic multiply-adds per training row of the 5 -> 256 -> 256 -> 256 -> 6
+# network with split (hi/lo) inputs: forward and weight-gradient products of
+# every layer, input-gradient products of layers 1-3 (the first layer needs none).
+MLP_LAYER_MACS = (10 * 256, 256 * 256, 256 * 256, 256 * 6)
+MLP_FLOP_PER_ROW = 2 * (2 * sum(MLP_LAYER_MACS) + sum(MLP_LAYER_MACS[1:]))
+
+
+def run_train(rows=1 << 17, batch=4096, epochs=8, seed=42, device=0):
+    """Surrogate training throughput: `epochs` passes of ismc_mlp_train_epoch
+    over device-resident synthetic rows (inputs sampled like the training set,
+    targets uniform in the outputs' ranges), after one warm-up epoch.  Each
+    epoch call returns after the device has finished (it checks the kernels'
+    error flag), so the host clock brackets the device work."""
+    import ctypes as C
+    import torch
+    from .surrogate import Surrogate, sample_inputs
+    rows = rows // batch * batch
+    rng = np.random.default_rng(seed)
+    X = sample_inputs(rows, seed=seed).astype(np.float32)
+    Y = np.stack([rng.uniform(0.0, 0.6, rows), rng.uniform(0.0, 0.6, rows),
+                  rng.uniform(0.0, 0.2, rows)], 1).astype(np.float32)
+    sur = Surrogate(device, max_batch=batch, seed=seed)
+    dX = torch.from_numpy(X).to(f"cuda:{device}")
+    dY = torch.from_numpy(Y).to(f"cuda:{device}")
+    torch.cuda.synchronize()
+    steps = rows // batch
+    lrs = np.full(steps, 1e-3, dtype=np.float32)
+    loss = C.c_float()
+
+    def epoch():
+        sur._check(sur.lib.ismc_mlp_train_epoch(sur.h, dX.data_ptr(), dY.data_ptr(), rows, batch,
+                                                lrs.ctypes.data_as(C.POINTER(C.c_float)),
+                                                C.byref(loss)))
+    epoch()
+    t0 = time.perf_counter()
+    for _ in range(epochs):
+        epoch()
+    dt = time.perf_counter() - t0
+    sur.close()
+    n_steps = epochs * steps
+    flop = MLP_FLOP_PER_ROW * batch
+    return {"rows": rows, "batch": batch, "epochs": epochs, "steps": n_steps, "seconds": dt,
+            "steps_per_s": n_steps / dt, "us_per_step": 1e6 * dt / n_steps,
+            "flop_per_step": flop, "tflops": flop * n_steps / dt / 1e12,
+            "launches_per_step": 14, "loss": float(loss.value)}
