@@ -9,7 +9,8 @@
 // (M x K) and B (N x K) both K-major BF16 in global memory, tiles brought into
 // shared memory by TMA (128-byte swizzle), multiplied by tcgen05.mma issued
 // from one thread into a TMEM accumulator (128 lanes x BN fp32 columns), and
-// read back by four warps with tcgen05.ld for a fused epilogue:
+// read back by eight warps with tcgen05.ld for a fused epilogue (one kernel
+// instantiation per epilogue mode):
 //   EPI_HIDDEN  z = acc + b;  H = silu(z) (row- and column-major bf16),
 //               G = silu'(z) (column-major bf16)
 //   EPI_BWD     dz = acc * G  (row- and column-major bf16), and the bias
@@ -18,8 +19,11 @@
 //   EPI_ACC     atomicAdd(acc) into fp32 (split-K weight gradients)
 // Each block of up to 64 columns is staged in the freed operand buffers, so
 // row-major outputs are written as whole 16-byte vectors and the split-K
-// gradients as coalesced atomics; column-major outputs are coalesced as
-// written (consecutive threads hold consecutive rows).
+// gradients as 16-byte vector atomics; column-major outputs are coalesced as
+// written (consecutive threads hold consecutive rows).  Every kernel of a
+// training step is launched with programmatic stream serialisation: its
+// set-up overlaps the previous kernel, and it waits (griddepcontrol.wait)
+// before its first global access.
 // Layer inputs are padded to K = 64 and the output layer to 16 rows, so every
 // product uses the same 64-wide K chunks.
 #include <cuda.h>
