@@ -44,10 +44,10 @@ def test_umma_gemm_matches_fp64(sur, M, N, K, splits):
     assert err <= GEMM_RTOL * scale, (err, scale)
 
 
-def test_mlp_gradients_vs_fp64_oracle(sur):
+@pytest.mark.parametrize("B", [512, 4096])      # 4096: the training batch's split-K choices
+def test_mlp_gradients_vs_fp64_oracle(sur, B):
     from oracle import mlp64
     rng = np.random.default_rng(0)
-    B = 512
     x = mlp64.LO + (mlp64.HI - mlp64.LO) * rng.random((B, 5))
     y = rng.random((B, 3)) * [0.5, 0.3, 0.2]
     p = sur.get_params().astype(np.float64)
