@@ -40,6 +40,7 @@ struct ismc_ctx {
     uint32_t g_n = 0;
     ismc_tune g_tune{0, 0, 0, 0};
     uint32_t g_cpw = 0;
+    uint32_t g_blocks = 0;
     char err[512] = {0};
 };
 
@@ -200,13 +201,35 @@ static int resolve_tune(ismc_ctx* ctx, const ismc_tune* req, ismc_tune* t, uint3
     return 0;
 }
 
+// Launch shape of a batch with fewer packets than half the tuned launch's
+// lanes: every packet its own lane, in full warps of 64-thread blocks spread
+// over the SMs, one queue chunk (32 packets) per warp.  Under the tuned shape
+// most warps would carry one or two live lanes yet issue every instruction,
+// and the schedulers' issue slots would be shared by all of them; a small
+// launch lasts as long as its longest packet, so its time per event is what
+// counts.  Results do not depend on the launch shape.
+static int small_batch_shape(ismc_ctx* ctx, uint64_t total, ismc_tune* t, uint32_t* blocks,
+                             uint32_t* cpw) {
+    const uint64_t lanes = (uint64_t)(*blocks) * t->block_threads;
+    if (total == 0 || total * 2 > lanes) return 0;
+    const uint32_t th = 64;
+    int bps = 0;
+    if (ismc_propagate_occupancy(th, &bps) != 0 || bps <= 0)
+        return set_err(ctx, ISMC_ERR_CUDA, "occupancy query failed for %u threads", th);
+    const uint64_t want = (total + th - 1) / th;
+    *blocks = (uint32_t)std::min<uint64_t>(want, (uint64_t)ctx->sms * (uint32_t)bps);
+    t->block_threads = th;
+    t->blocks_per_sm = 0;
+    *cpw = 1;
+    return 0;
+}
+
 static int enqueue_pipeline(ismc_ctx* ctx, const ismc_instance* d_in, uint32_t n,
-                            const ismc_tune& t, uint32_t blocks, ismc_tally* d_out,
+                            const ismc_tune& t, uint32_t blocks, uint32_t cpw, ismc_tally* d_out,
                             cudaStream_t s) {
     const uint32_t warps = blocks * (t.block_threads / 32);
     int rc = ismc_launch_prepare(d_in, n, ctx->d_inst, ctx->d_range, ctx->d_prefix, d_out,
-                                 ctx->d_ctrl, t.chunk_packets, warps, ctx->chunks_per_warp,
-                                 (void*)s);
+                                 ctx->d_ctrl, t.chunk_packets, warps, cpw, (void*)s);
     if (rc) return set_err(ctx, rc, "prepare launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     PropParams p;
     p.inst = ctx->d_inst;
@@ -257,7 +280,8 @@ extern "C" int ismc_run_batch_device(ismc_ctx* ctx, const ismc_instance* d_inst,
     if (rc) return rc;
     // the caller's stream exactly as given (NULL = the legacy default stream),
     // so the launch is ordered with the caller's own copies and events
-    return enqueue_pipeline(ctx, d_inst, n_inst, t, blocks, d_out, (cudaStream_t)stream);
+    return enqueue_pipeline(ctx, d_inst, n_inst, t, blocks, ctx->chunks_per_warp, d_out,
+                            (cudaStream_t)stream);
 }
 
 static bool same_tune(const ismc_tune& a, const ismc_tune& b) {
@@ -279,16 +303,21 @@ extern "C" int ismc_run_batch(ismc_ctx* ctx, const ismc_instance* inst, uint32_t
     uint32_t blocks;
     rc = resolve_tune(ctx, tune, &t, &blocks);
     if (rc) return rc;
+    uint32_t cpw = ctx->chunks_per_warp;
+    if (!tune || tune->block_threads == 0) {
+        rc = small_batch_shape(ctx, total_packets(inst, n_inst), &t, &blocks, &cpw);
+        if (rc) return rc;
+    }
     memcpy(ctx->h_in, inst, sizeof(ismc_instance) * n_inst);
     // replay the captured pipeline when batch size and launch shape repeat
-    if (!(ctx->gexec && ctx->g_n == n_inst && same_tune(ctx->g_tune, t) &&
-          ctx->g_cpw == ctx->chunks_per_warp)) {
+    if (!(ctx->gexec && ctx->g_n == n_inst && same_tune(ctx->g_tune, t) && ctx->g_cpw == cpw &&
+          ctx->g_blocks == blocks)) {
         if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         cudaMemcpyAsync(ctx->d_in, ctx->h_in, sizeof(ismc_instance) * n_inst,
                         cudaMemcpyHostToDevice, ctx->stream);
-        int rc2 = enqueue_pipeline(ctx, ctx->d_in, n_inst, t, blocks, ctx->d_out, ctx->stream);
+        int rc2 = enqueue_pipeline(ctx, ctx->d_in, n_inst, t, blocks, cpw, ctx->d_out, ctx->stream);
         cudaMemcpyAsync(ctx->h_out, ctx->d_out, sizeof(ismc_tally) * n_inst,
                         cudaMemcpyDeviceToHost, ctx->stream);
         cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
@@ -301,7 +330,8 @@ extern "C" int ismc_run_batch(ismc_ctx* ctx, const ismc_instance* inst, uint32_t
             return set_err(ctx, ISMC_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
         ctx->g_n = n_inst;
         ctx->g_tune = t;
-        ctx->g_cpw = ctx->chunks_per_warp;
+        ctx->g_cpw = cpw;
+        ctx->g_blocks = blocks;
     }
     CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -376,7 +406,7 @@ extern "C" int ismc_autotune(ismc_ctx* ctx, const ismc_instance* inst, uint32_t 
             float best_ms = 1e30f;
             for (int rep = 0; rep < 2; ++rep) {
                 CK(cudaEventRecord(tr.e0, ctx->stream));
-                rc = enqueue_pipeline(ctx, ctx->d_in, n_inst, r, blocks, ctx->d_out, ctx->stream);
+                rc = enqueue_pipeline(ctx, ctx->d_in, n_inst, r, blocks, cpw, ctx->d_out, ctx->stream);
                 if (rc) return rc;
                 CK(cudaEventRecord(tr.e1, ctx->stream));
                 CK(cudaEventSynchronize(tr.e1));
