@@ -69,6 +69,12 @@ def test_gpu_launch_shape_invariance(engine):
     for bt, chunk in ((128, 32), (256, 1000), (512, 96), (384, 65536), (64, 7)):
         got = engine.run_batch_raw([inst], make_tune(bt, 0, chunk, 0))[0]
         assert _same(got, ref), (bt, chunk)
+    # a batch below half the tuned launch's lanes runs one packet per lane when
+    # no shape is requested: the same tallies as under requested shapes
+    small = cases.case_instance(c, 5_000, seed=9)
+    auto = engine.run_batch_raw([small])[0]
+    for bt in (64, 512):
+        assert _same(engine.run_batch_raw([small], make_tune(bt, 0, 0, 0))[0], auto), bt
 
 
 def test_gpu_uneven_batch_equals_single_runs(engine):
