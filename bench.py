@@ -477,7 +477,7 @@ def run_other_workload(args):
                 "roofline": {"bound": "tensor", "unit": "TFLOP/s", "achieved": r["tflops"],
                              "peak": peak, "frac": r["tflops"] / peak if peak else None,
                              "traffic": None,
-                             "note": "algorithmic FLOP per step over host-timed steps (14 "
+                             "note": "algorithmic FLOP per step over host-timed steps (13 "
                                      "launches each); peak = measured bf16 burst "
                                      "(MEASURED_PEAKS.json, of measured)"},
                 "result": r}

@@ -230,4 +230,4 @@ def run_train(rows=1 << 17, batch=4096, epochs=8, seed=42, device=0):
     return {"rows": rows, "batch": batch, "epochs": epochs, "steps": n_steps, "seconds": dt,
             "steps_per_s": n_steps / dt, "us_per_step": 1e6 * dt / n_steps,
             "flop_per_step": flop, "tflops": flop * n_steps / dt / 1e12,
-            "launches_per_step": 14, "loss": float(loss.value)}
+            "launches_per_step": 13, "loss": float(loss.value)}

@@ -16,6 +16,9 @@
 //   EPI_BWD     dz = acc * G  (row- and column-major bf16), and the bias
 //               gradient as column sums of dz
 //   EPI_OUT     z = acc + b   (fp32)
+//   EPI_LOSS    z = acc + b, and straight from it the Gaussian NLL of each row,
+//               its gradient dO (row- and column-major bf16) and the output
+//               bias gradient (training: the loss needs no kernel of its own)
 //   EPI_ACC     atomicAdd(acc) into fp32 (split-K weight gradients)
 // Each block of up to 64 columns is staged in the freed operand buffers, so
 // row-major outputs are written as whole 16-byte vectors and the split-K
@@ -51,7 +54,7 @@ constexpr uint32_t WAIT_LIMIT = 1u << 22;   // polls of a bounded try_wait: seco
 // each for half of the tile's columns
 constexpr int GEMM_THREADS = 256;
 
-enum { EPI_HIDDEN = 0, EPI_BWD = 1, EPI_OUT = 2, EPI_ACC = 3 };
+enum { EPI_HIDDEN = 0, EPI_BWD = 1, EPI_OUT = 2, EPI_ACC = 3, EPI_LOSS = 4 };
 
 struct Epi {
     int mode;
@@ -69,6 +72,9 @@ struct Epi {
     float* out_f;                  // [M x ldf]
     int ldf;
     int fold;                      // EPI_ACC: columns n and n + fold accumulate into n (0: none)
+    const float* target;           // EPI_LOSS: targets y [M x 3]
+    float* loss;                   // EPI_LOSS: += mean loss
+    float inv_m, floor2;           // EPI_LOSS: 1 / rows of the batch, variance floor squared
 };
 
 // 1 / (1 + e^-z); the fast divide returns 0 once e^-z passes 2^126, the limit anyway
@@ -249,7 +255,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(const __grid
                     dst[0] = reinterpret_cast<const uint4*>(o)[0];
                     dst[1] = reinterpret_cast<const uint4*>(o)[1];
                 } else {
-                    if constexpr (MODE == EPI_OUT) {
+                    if constexpr (MODE == EPI_OUT || MODE == EPI_LOSS) {
 #pragma unroll
                         for (int j = 0; j < 16; ++j) v[j] += pre[j];
                     }
@@ -280,6 +286,53 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(const __grid
                             acc += __bfloat162float(sb[row * SB + col]);
                         atomicAdd(e.bias_grad + n0 + cb + col, acc);
                     }
+                }
+            } else if constexpr (MODE == EPI_LOSS) {
+                // Gaussian NLL with a variance floor, one thread per row, from the
+                // staged outputs z (mu in columns 0-2, log-variance s in 3-5):
+                //   v = e^s + floor^2,  loss = mean_rows sum_k 0.5 (d^2 / v + ln v),  d = y - mu
+                //   dloss/dmu = -d / v,  dloss/ds = 0.5 (e^s / v) (1 - d^2 / v)
+                // dO gets columns 0-15 of its row (6-15 zero; 16-63 stay zero
+                // from creation) and dOT rows 0-5; the loss and the output bias
+                // gradient (sums of the rounded dO) are reduced over the block.
+                float part[7] = {0, 0, 0, 0, 0, 0, 0};
+                const int gr = m0 + (int)threadIdx.x;
+                if (threadIdx.x < BM && gr < e.M) {
+                    const float* zr = sf + threadIdx.x * SF;
+                    __align__(16) __nv_bfloat16 o[16];
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) o[k] = __float2bfloat16_rn(0.0f);
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        const float mu = zr[q], es = __expf(zr[3 + q]);
+                        const float d = e.target[(size_t)gr * 3 + q] - mu;
+                        const float vv = es + e.floor2, iv = 1.0f / vv;
+                        part[0] += 0.5f * (d * d * iv + __logf(vv));
+                        o[q] = __float2bfloat16_rn(-d * iv * e.inv_m);
+                        o[3 + q] = __float2bfloat16_rn(0.5f * es * iv * (1.0f - d * d * iv) * e.inv_m);
+                    }
+                    uint4* dst = reinterpret_cast<uint4*>(e.out_row + (size_t)gr * e.ldr);
+                    dst[0] = reinterpret_cast<const uint4*>(o)[0];
+                    dst[1] = reinterpret_cast<const uint4*>(o)[1];
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) {
+                        e.out_col[(size_t)k * e.ldc + gr] = o[k];
+                        part[1 + k] = __bfloat162float(o[k]);
+                    }
+                }
+                float* red = sf + BM * SF;                  // [8 warps][7], past the staged rows
+#pragma unroll
+                for (int k = 0; k < 7; ++k) {
+                    for (int off = 16; off > 0; off >>= 1)
+                        part[k] += __shfl_down_sync(0xFFFFFFFFu, part[k], off);
+                    if (lane == 0) red[warp * 7 + k] = part[k];
+                }
+                __syncthreads();
+                if (threadIdx.x < 7) {
+                    float t = 0.0f;
+                    for (int w = 0; w < GEMM_THREADS / 32; ++w) t += red[w * 7 + threadIdx.x];
+                    if (threadIdx.x == 0) atomicAdd(e.loss, t * e.inv_m);
+                    else atomicAdd(e.bias_grad + threadIdx.x - 1, t);
                 }
             } else if (MODE == EPI_ACC && e.fold) {
                 // the input's hi and lo columns n and n + fold share a weight
@@ -347,7 +400,7 @@ __global__ void prep_inputs(const float* __restrict__ x, int B, Norm nm, __nv_bf
     umma::grid_dep_wait();
     umma::grid_dep_launch();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r == 0) *loss = 0.0f;      // the step's loss accumulates from here (nll_loss_grad)
+    if (r == 0) *loss = 0.0f;      // the step's loss accumulates from here (output epilogue)
     if (r >= B) return;
     __align__(16) __nv_bfloat16 o[16];
 #pragma unroll
@@ -363,66 +416,6 @@ __global__ void prep_inputs(const float* __restrict__ x, int B, Norm nm, __nv_bf
     dst[1] = reinterpret_cast<const uint4*>(o)[1];
 #pragma unroll
     for (int k = 0; k < 10; ++k) X0T[(size_t)k * B + r] = o[k];
-}
-
-// Gaussian NLL with a variance floor: out O [B x 16] fp32 (mu in cols 0-2,
-// log-variance s in 3-5), targets y [B x 3], variance v = exp(s) + floor^2:
-//   loss = mean_b sum_k 0.5 (d^2 / v + ln v),  d = y - mu
-//   dloss/dmu = -d / v,  dloss/ds = 0.5 (e^s / v) (1 - d^2 / v).
-// The floor (the training targets' Monte Carlo noise scale) keeps the
-// per-sample precision weights bounded where the targets are noise-free
-// (e.g. T_u = 0 for thick samples); floor = 0 is the plain Gaussian NLL.
-// dO (bf16 [B x 64] row, [64 x B] column) = dloss/dO: columns 0-15 of dO are
-// written (6-15 as zeros; 16-63 stay zero from creation) and rows 0-5 of dOT.
-// The output layer's bias gradient db[k] = sum_b bf16(dO[b][k]) is reduced here
-// too (block sums, one atomic per block and column).
-__global__ void nll_loss_grad(const float* __restrict__ O, const float* __restrict__ y, int B,
-                              float inv_b, float floor2, __nv_bfloat16* dO, __nv_bfloat16* dOT,
-                              float* loss, float* db) {
-    umma::grid_dep_wait();
-    umma::grid_dep_launch();
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    float part[7] = {0, 0, 0, 0, 0, 0, 0};      // loss, then the six bias-gradient columns
-    if (r < B) {
-        __align__(16) __nv_bfloat16 o[16];
-#pragma unroll
-        for (int k = 0; k < 16; ++k) o[k] = __float2bfloat16_rn(0.0f);
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            const float mu = O[(size_t)r * 16 + q], s = O[(size_t)r * 16 + 3 + q];
-            const float d = y[(size_t)r * 3 + q] - mu;
-            const float es = __expf(s);
-            const float v = es + floor2;
-            const float iv = 1.0f / v;
-            part[0] += 0.5f * (d * d * iv + __logf(v));
-            o[q] = __float2bfloat16_rn(-d * iv * inv_b);
-            o[3 + q] = __float2bfloat16_rn(0.5f * es * iv * (1.0f - d * d * iv) * inv_b);
-        }
-        uint4* dst = reinterpret_cast<uint4*>(dO + (size_t)r * 64);
-        dst[0] = reinterpret_cast<const uint4*>(o)[0];
-        dst[1] = reinterpret_cast<const uint4*>(o)[1];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            dOT[(size_t)k * B + r] = o[k];
-            part[1 + k] = __bfloat162float(o[k]);
-        }
-    }
-    // block reduction: warp shuffles, then one row of partial sums per warp
-    __shared__ float red[32][7];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < 7; ++k)
-        for (int off = 16; off > 0; off >>= 1) part[k] += __shfl_down_sync(0xFFFFFFFFu, part[k], off);
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < 7; ++k) red[warp][k] = part[k];
-    __syncthreads();
-    if (threadIdx.x < 7) {
-        float t = 0.0f;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][threadIdx.x];
-        if (threadIdx.x == 0) atomicAdd(loss, t * inv_b);
-        else atomicAdd(db + threadIdx.x - 1, t);
-    }
 }
 
 // The parameter tensors of one Adam step, in the flat buffers' order: each
@@ -631,6 +624,9 @@ static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, 
                        const Epi& e, int splits = 1) {
     // A: [M x K] bf16, B: [N x K] bf16, both K-major; M % 128 == 0, N % BN == 0, K % 64 == 0
     if (e.mode != MODE) return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: epilogue mode mismatch");
+    // the loss epilogue: one 16-column tile holding all six outputs, whole rows
+    if (MODE == EPI_LOSS && (BN != 16 || N != 16 || e.N != 6 || e.M != M || e.ldr != 64))
+        return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: loss epilogue needs the 16-column output tile");
     // folded gradient columns: both halves in the first (only) block of one tile
     if (e.fold && (MODE != EPI_ACC || N != BN || e.N != 2 * e.fold || e.N > (BN < 64 ? BN : 64)))
         return mlp_err(m, ISMC_ERR_INTERNAL, "gemm: folded columns must share one tile");
@@ -802,8 +798,11 @@ extern "C" int ismc_mlp_set_params(ismc_mlp* m, const float* host, size_t n) {
     return 0;
 }
 
-// forward pass of B rows of raw inputs; leaves H, G and O in the workspace
-static int forward(ismc_mlp* m, const float* d_x, int B) {
+// Forward pass of B rows of raw inputs; leaves H and G in the workspace.
+// Without targets the outputs go to O; with targets d_y the output layer's
+// epilogue computes the loss (into m->d_loss, cleared by prep_inputs), its
+// gradient dO / dOT and the output bias gradient instead.
+static int forward(ismc_mlp* m, const float* d_x, int B, const float* d_y = nullptr) {
     MCK(launch_pdl(prep_inputs, dim3((B + 127) / 128), dim3(128), m->stream, d_x, B, g_norm, m->X0,
                    m->X0T, m->d_loss));
     const __nv_bfloat16* in = m->X0;
@@ -821,19 +820,28 @@ static int forward(ismc_mlp* m, const float* d_x, int B) {
         K = 256;
     }
     Epi e{};
-    e.mode = EPI_OUT; e.M = B; e.N = 6;
+    e.M = B; e.N = 6;
     e.bias = m->d_w + m->off_b[3];
-    e.out_f = m->O; e.ldf = 16;
-    return launch_gemm<16, EPI_OUT>(m, in, B, 256, m->Wb[3], 16, e);
+    if (!d_y) {
+        e.mode = EPI_OUT;
+        e.out_f = m->O; e.ldf = 16;
+        return launch_gemm<16, EPI_OUT>(m, in, B, 256, m->Wb[3], 16, e);
+    }
+    e.mode = EPI_LOSS;
+    e.target = d_y;
+    e.loss = m->d_loss;
+    e.inv_m = 1.0f / B;
+    e.floor2 = kVarFloor * kVarFloor;
+    e.out_row = m->dO; e.ldr = 64;
+    e.out_col = m->dOT; e.ldc = B;
+    e.bias_grad = m->d_g + m->off_b[3];
+    return launch_gemm<16, EPI_LOSS>(m, in, B, 256, m->Wb[3], 16, e);
 }
 
-// gradients of the mean loss added into m->d_g, which holds zeros on entry (it
-// is cleared at creation, by each Adam step and after ismc_mlp_grad), and the
-// loss into m->d_loss (cleared by prep_inputs)
-static int backward(ismc_mlp* m, const float* d_y, int B) {
-    MCK(launch_pdl(nll_loss_grad, dim3((B + 255) / 256), dim3(256), m->stream, (const float*)m->O,
-                   d_y, B, 1.0f / B, kVarFloor * kVarFloor, m->dO, m->dOT, m->d_loss,
-                   m->d_g + m->off_b[3]));
+// Gradients of the mean loss added into m->d_g, which holds zeros on entry (it
+// is cleared at creation, by each Adam step and after ismc_mlp_grad), after a
+// forward pass with targets (which produced dO, dOT and the output bias gradient).
+static int backward(ismc_mlp* m, int B) {
     // split-K over the batch for the weight gradients: about 128 CTAs per
     // product (a power of two of 64-row slices that divides the batch)
     auto splits_for = [B](int tiles) {
@@ -905,9 +913,9 @@ extern "C" int ismc_mlp_grad(ismc_mlp* m, const float* d_x, const float* d_y, ui
     if (!m || !d_x || !d_y || B == 0 || B % 128 || (int)B > m->max_batch)
         return ISMC_ERR_INVALID_ARG;
     MCK(cudaSetDevice(m->device));
-    int rc = forward(m, d_x, (int)B);
+    int rc = forward(m, d_x, (int)B, d_y);
     if (rc) return rc;
-    rc = backward(m, d_y, (int)B);
+    rc = backward(m, (int)B);
     if (rc) return rc;
     if (d_grad) MCK(cudaMemcpyAsync(d_grad, m->d_g, m->nparam * 4, cudaMemcpyDeviceToDevice, m->stream));
     if (loss) MCK(cudaMemcpyAsync(loss, m->d_loss, 4, cudaMemcpyDeviceToHost, m->stream));
@@ -921,9 +929,9 @@ extern "C" int ismc_mlp_train_step(ismc_mlp* m, const float* d_x, const float* d
     if (!m || !d_x || !d_y || B == 0 || B % 128 || (int)B > m->max_batch)
         return ISMC_ERR_INVALID_ARG;
     MCK(cudaSetDevice(m->device));
-    int rc = forward(m, d_x, (int)B);
+    int rc = forward(m, d_x, (int)B, d_y);
     if (rc) return rc;
-    rc = backward(m, d_y, (int)B);
+    rc = backward(m, (int)B);
     if (rc) return rc;
     ++m->adam_t;
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
