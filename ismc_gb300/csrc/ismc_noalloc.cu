@@ -109,8 +109,10 @@ extern "C" int ismc_run_batch_noalloc(const ismc_instance* d_inst, uint32_t n_in
     // the prepare and scan kernels rewrite every scratch word the propagator
     // reads (tables, ranges, prefix, queue head, chunk size) and zero the
     // caller's tallies, so nothing left from an earlier call is used
+    // 32 queue chunks per warp when the chunk size is left to the device: the
+    // context entry points' default, which shortens the end-of-launch tail
     rc = ismc_launch_prepare(d_inst, n_inst, S->inst, S->range, S->prefix, d_out, S->ctrl,
-                             tune ? tune->chunk_packets : 0u, warps, 8u, stream);
+                             tune ? tune->chunk_packets : 0u, warps, 32u, stream);
     if (rc)
         return ismc_lib_error(rc, "run_batch_noalloc: prepare launch failed: %s",
                               cudaGetErrorString(cudaGetLastError()));
