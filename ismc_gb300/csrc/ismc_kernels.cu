@@ -569,8 +569,7 @@ ismc_propagate_kernel(const PropParams P) {
                 const int nl = down ? l + 1 : l - 1;
                 const float eta = down ? q2.w : q2.z;
                 float ct;
-                const float R = ismc_fresnel(eta, auz, &ct);
-                if (u0 < R) {
+                if (ismc_fresnel_reflects(eta, auz, u0, &ct)) {
                     uz = -uz;
                 } else if (nl < 0 || nl >= (int)L) {
                     side = nl < 0 ? 0u : 1u;

@@ -178,6 +178,22 @@ __device__ __forceinline__ float ismc_fresnel(float eta, float ci, float* ct) {
     return __fdiv_rn(0.5f * __fmaf_rn(x, x, y * y), den * den);
 }
 
+// The reflect-or-transmit draw u < ismc_fresnel(eta, ci, ct) without the
+// division: with R = N / D and D = den^2 > 0, u < R exactly when u D < N in
+// real arithmetic (the rounded forms can differ only where the division's
+// rounding would flip the comparison).  A total internal reflection always
+// reflects, since u < 1.
+__device__ __forceinline__ bool ismc_fresnel_reflects(float eta, float ci, float u, float* ct) {
+    const float s2t = (eta * eta) * (1.0f - ci * ci);
+    if (s2t >= 1.0f) { *ct = 0.0f; return true; }
+    const float c = __fsqrt_rn(1.0f - s2t);
+    const float a = eta * ci, b = eta * c;
+    const float rsn = a - c, rsd = a + c, rpn = b - ci, rpd = b + ci;
+    const float x = rsn * rpd, y = rpn * rsd, den = rsd * rpd;
+    *ct = c;
+    return u * (den * den) < 0.5f * __fmaf_rn(x, x, y * y);
+}
+
 // Fixed-point quantisation of a non-negative packet weight (scale 2^32).
 __device__ __forceinline__ unsigned long long ismc_q32(float x) {
     return __float2ull_rn(x * 4294967296.0f);

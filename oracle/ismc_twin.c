@@ -119,6 +119,19 @@ static float fresnel(float eta, float ci, float* ct) {
     return (0.5f * fmaf(x, x, y * y)) / (den * den);
 }
 
+/* The draw u < fresnel(eta, ci, ct) without the division, as the GPU takes
+ * it at an interface: u * den^2 < (x^2 + y^2) / 2. */
+static int fresnel_reflects(float eta, float ci, float u, float* ct) {
+    const float s2t = (eta * eta) * (1.0f - ci * ci);
+    if (s2t >= 1.0f) { *ct = 0.0f; return 1; }
+    const float c = sqrtf(1.0f - s2t);
+    const float a = eta * ci, b = eta * c;
+    const float rsn = a - c, rsd = a + c, rpn = b - ci, rpd = b + ci;
+    const float x = rsn * rpd, y = rpn * rsd, den = rsd * rpd;
+    *ct = c;
+    return u * (den * den) < 0.5f * fmaf(x, x, y * y);
+}
+
 static inline uint64_t q32(float x) { return (uint64_t)llrintf(x * 4294967296.0f); }
 
 /* ------------------------------------------------------------ instance prep */
@@ -268,8 +281,7 @@ static void run_packet(const TwinInst* I, uint64_t id, uint32_t max_events, Twin
                 const int nl = down ? l + 1 : l - 1;
                 const float eta = down ? I->eta_dn[l] : I->eta_up[l];
                 float ct;
-                const float R = fresnel(eta, auz, &ct);
-                if (u0 < R) {
+                if (fresnel_reflects(eta, auz, u0, &ct)) {
                     uz = -uz;
                 } else if (nl < 0 || nl >= (int)I->L) {
                     side = nl < 0 ? 0 : 1;
