@@ -167,6 +167,9 @@ int ismc_run(ismc_ctx* ctx, const ismc_stack* stack, const ismc_spheres* sph,
  * CUDA/ISMLMC-lookup.cu:153-421 (singleLayerSampleSpace), lookup.py:228-259
  * (sample_space) and the per-objective launches of
  * CUDA/ISMLMC-minimization.cu:89-131 (cost).  out has n_inst entries.
+ * With tune NULL (or block_threads 0), a batch of fewer packets than half the
+ * tuned launch's lanes runs one packet per lane in 64-thread blocks; the
+ * tallies do not depend on the launch shape.
  */
 int ismc_run_batch(ismc_ctx* ctx, const ismc_instance* inst, uint32_t n_inst,
                    const ismc_tune* tune, ismc_tally* out);
