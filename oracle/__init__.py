@@ -49,6 +49,8 @@ def lib():
         L.twin_expneg.argtypes = [C.c_float]
         L.twin_fresnel.restype = C.c_float
         L.twin_fresnel.argtypes = [C.c_float, C.c_float, P(C.c_float)]
+        L.twin_fresnel_reflects.restype = C.c_int
+        L.twin_fresnel_reflects.argtypes = [C.c_float, C.c_float, C.c_float, P(C.c_float)]
         L.ref64_run.restype = C.c_int
         L.ref64_run.argtypes = [C.c_int, P(_abi.Instance), C.c_int, P(C.c_double),
                                 P(C.c_double), P(C.c_uint64)]

@@ -465,3 +465,6 @@ float twin_neglog_u32(uint32_t x) { return neglog_u32(x); }
 void twin_sincos_2pi(float u, float* s, float* c) { sincos_2pi(u, s, c); }
 float twin_expneg(float x) { return expneg(x); }
 float twin_fresnel(float eta, float ci, float* ct) { return fresnel(eta, ci, ct); }
+int twin_fresnel_reflects(float eta, float ci, float u, float* ct) {
+    return fresnel_reflects(eta, ci, u, ct);
+}

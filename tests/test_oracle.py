@@ -222,6 +222,33 @@ def test_fresnel_algebraic_equals_trigonometric():
             assert abs(got - ref) < 2e-5, (ni, nt, mz, got, ref)
 
 
+def test_twin_interface_draw_without_division_matches_u_below_R():
+    """The interface draw u * den^2 < (x^2 + y^2)/2 (no division) decides as
+    u < R does, except where u lies within rounding of R; and it hands back
+    the same refracted cosine."""
+    import ctypes as C
+    L = oracle.lib()
+    ct, ct2 = C.c_float(), C.c_float()
+    rng = np.random.default_rng(12)
+    mism = 0
+    for ni, nt in ((1.0, 1.4), (1.4, 1.0), (1.37, 1.52), (1.52, 1.0), (1.44, 1.52)):
+        eta = float(np.float32(ni / nt))
+        ci = rng.uniform(1e-4, 1.0, 4000).astype(np.float32)
+        for c in ci:
+            R = L.twin_fresnel(eta, float(c), C.byref(ct))
+            # u on both sides of R, and right next to it
+            for u in (R * 0.5, R * (1 - 1e-6), R * (1 + 1e-6), min(0.99999994, R + (1 - R) * 0.5)):
+                u = float(np.float32(u))
+                if not 0.0 < u < 1.0:
+                    continue
+                got = bool(L.twin_fresnel_reflects(eta, float(c), u, C.byref(ct2)))
+                assert ct2.value == ct.value
+                if got != (u < R):
+                    mism += 1
+                    assert abs(u - R) <= 4e-7 * max(R, 1e-30), (ni, nt, c, u, R)
+    assert mism <= 20, mism
+
+
 # ----------------------------------------------------------------------------
 # FP64 analytic oracle
 # ----------------------------------------------------------------------------
