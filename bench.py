@@ -1,28 +1,37 @@
 """Benchmark of the GB300 photon propagator.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+                    [--stack bench1|bench1_noslides|bench0|bench0_noslides]
 
 Workload (one "step"): the three-layer stack between n = 1.52 slides
 (n=1.37/1.40/1.44, mua=0.5/2.0/0.2 1/cm, mus=200/120/50 1/cm, g=0.8/0.9/0.75,
 d=0.01/0.15/0.3 cm; slides 0.1 cm), two 5.08 cm spheres with 1.27/1.27/0.635 cm
 ports and wall reflectance 0.98, crosstalk on, 1e8 photon packets, seed 7 --
-one full forward simulation.  Metric: photons/s.
+one full forward simulation.  Metric: photons/s.  --stack picks another stack
+of the same geometry for comparisons (the single-slab configuration, or either
+stack without its slides).
 
 GPU arm (default): `value` is timed with CUDA events around the device-pointer
 entry point (instances already in HBM); `e2e` times the host-pointer C ABI call
 (ismc_run_batch: H2D of the instance, prepare, scan, propagate, D2H of the
 tally) with a host clock.  L2 is flushed (a 512 MB write) before every timed
 step.  Under torchrun each rank simulates its own packet range of the same
-stack (weak scaling) and the max time over ranks is reported.
+stack (weak scaling), the max time over ranks is reported, and the ranks'
+integer tallies are summed into the merged result; a reduced-size sharded run
+is checked bit for bit against a single-process run of the same range.
 
 Reference arm (--impl reference): the reference's algorithm on the host cores,
 as restated in FP64 C from ISMLMC.py / MLMC.py (oracle/ismc_ref64.c: the
 reference itself is Python and cannot run on the GPU machine), each step a
 bounded packet sample of the same workload.
+Reference CUDA arm (--impl reference --workload refcuda): the reference's own
+CUDA kernel and host entry point (CUDA/CUDAISMLMC.h, compiled unmodified from a
+staged copy by oracle/build_ref.py) on the same GPU, in calls of 1e7 packets.
 """
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -37,13 +46,36 @@ PACKETS = 100_000_000
 SEED = 7
 L2_FLUSH_BYTES = 512 << 20
 ROOFLINE_FILE = os.path.join(ROOT, "profiles", "propagator_bench1_roofline.json")
+# packets per call of the reference's CUDA entry point: its curand-state array
+# holds RNGS = 2e7 states and N/256 + 1 blocks of 256 threads use one each
+# (CUDA/CUDAISMLMC.h:12, 660-683)
+REFCUDA_PACKETS_PER_CALL = 10_000_000
 
 
-def workload_layers():
-    from ismc_gb300 import Layer
-    return [Layer.slide(1.52, 0.1), Layer(1.37, 0.5, 200.0, 0.8, 0.01),
-            Layer(1.40, 2.0, 120.0, 0.9, 0.15), Layer(1.44, 0.2, 50.0, 0.75, 0.3),
-            Layer.slide(1.52, 0.1)]
+def _layers(stack):
+    from ismc_gb300 import workloads as W
+    if stack == "bench1":
+        return W.bench1_layers()
+    if stack == "bench1_noslides":
+        return W.bench1_layers()[1:4]
+    if stack == "bench0":
+        return W.bench0_layers()
+    if stack == "bench0_noslides":
+        return W.bench0_layers()[1:2]
+    raise ValueError(f"unknown stack {stack!r}")
+
+
+STACK_TEXT = {
+    "bench1": "3-layer stack between n=1.52 slides (the multilayer benchmark configuration)",
+    "bench1_noslides": "the multilayer benchmark's 3 tissue layers without the slides",
+    "bench0": "one slab (n 1.4, mua 1, mus 100, g 0.9, d 0.1 cm) between n=1.5 slides "
+              "(the single-layer configuration)",
+    "bench0_noslides": "the single-layer configuration's slab without the slides",
+}
+
+
+def workload_layers(stack="bench1"):
+    return _layers(stack)
 
 
 def workload_spheres():
@@ -51,16 +83,20 @@ def workload_spheres():
     return Spheres.from_radii(5.08, 1.27, 1.27, 0.635, 0.98, R=True, T=True)
 
 
-def workload_instance(n, offset=0):
+def workload_instance(n, offset=0, stack="bench1"):
     from ismc_gb300 import make_instance
-    return make_instance(workload_layers(), workload_spheres(), n, seed=SEED, mode="compat",
+    return make_instance(workload_layers(stack), workload_spheres(), n, seed=SEED, mode="compat",
                          roulette_threshold=1e-4, roulette_m=10.0, packet_offset=offset)
 
 
-CONFIG = {"workload": "3-layer stack between n=1.52 slides, two 5.08 cm spheres with crosstalk, "
-                      "1e8 packets per step (the multilayer benchmark configuration)",
-          "layers": 5, "packets_per_step": PACKETS, "seed": SEED, "mode": "compat",
-          "l2": "flushed (512 MB write) before every timed step"}
+def workload_config(stack="bench1", packets=PACKETS):
+    return {"workload": f"{STACK_TEXT[stack]}, two 5.08 cm spheres with crosstalk, "
+                        f"{packets:.0e} packets per step", "stack": stack,
+            "layers": len(workload_layers(stack)), "packets_per_step": packets, "seed": SEED,
+            "mode": "compat", "l2": "flushed (512 MB write) before every timed step"}
+
+
+CONFIG = workload_config()
 
 
 # ----------------------------------------------------------------------------
@@ -114,18 +150,18 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def cpu_baseline(seconds=12.0):
+def cpu_baseline(seconds=12.0, stack="bench1"):
     """The reference's algorithm (FP64 restatement of ISMLMC.py) on all host
     cores, on a bounded packet sample of the workload."""
     import oracle
     threads = os.cpu_count()
     n = 20000
     t0 = time.perf_counter()
-    oracle.ref64_run(workload_instance(n), threads=threads)
+    oracle.ref64_run(workload_instance(n, stack=stack), threads=threads)
     dt = time.perf_counter() - t0
     n2 = max(n, int(n * seconds / max(dt, 1e-3)))
     t0 = time.perf_counter()
-    _, _, steps = oracle.ref64_run(workload_instance(n2), threads=threads)
+    _, _, steps = oracle.ref64_run(workload_instance(n2, stack=stack), threads=threads)
     dt = time.perf_counter() - t0
     return {"value": n2 / dt, "unit": "photons/s", "cores": threads, "kind": "port",
             "sample": f"{n2} packets of the workload (FP64 C restatement of ISMLMC.py/MLMC.py, "
@@ -309,17 +345,19 @@ def run_reference(args, rank, world):
     threads = os.cpu_count()
     # size one step to ~10 s of host work
     n = 20000
+    st = args.stack
     t0 = time.perf_counter()
-    oracle.ref64_run(workload_instance(n), threads=threads)
+    oracle.ref64_run(workload_instance(n, stack=st), threads=threads)
     dt = time.perf_counter() - t0
     per_step = max(n, int(n * 10.0 / max(dt, 1e-3)))
     for w in range(args.warmup):
-        oracle.ref64_run(workload_instance(min(per_step, 20000), offset=w * per_step),
+        oracle.ref64_run(workload_instance(min(per_step, 20000), offset=w * per_step, stack=st),
                          threads=threads)
     times = []
     for k in range(args.steps):
         t0 = time.perf_counter()
-        oracle.ref64_run(workload_instance(per_step, offset=k * per_step), threads=threads)
+        oracle.ref64_run(workload_instance(per_step, offset=k * per_step, stack=st),
+                         threads=threads)
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = per_step * args.steps / total
@@ -327,13 +365,87 @@ def run_reference(args, rank, world):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": dict(CONFIG, packets_per_step=per_step,
+            "config": dict(workload_config(st, args.packets), packets_per_step=per_step,
                            note="each step is a bounded packet sample of the workload"),
             "cpu_baseline": {"value": value, "unit": "photons/s", "cores": threads, "kind": "port",
                              "sample": f"{per_step} packets per step, FP64 C restatement of "
                                        f"ISMLMC.py/MLMC.py on {threads} threads"},
             "e2e": {"value": value, "unit": "photons/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_refcuda(args, rank):
+    """The reference's own CUDA forward model on this GPU (--impl reference
+    --workload refcuda): kernel CUDAISMLMC timed alone with CUDA events, and the
+    reference's host entry point ISMLMC() timed with a host clock, both on the
+    chosen stack, in calls of 1e7 packets (oracle/refcuda_bench.cu)."""
+    if rank != 0:
+        return
+    st = args.stack
+    base = {"impl": "reference", "workload": "refcuda", "metric": "photons/s", "unit": "photons/s",
+            "config": workload_config(st, args.packets)}
+    if st not in ("bench1_noslides", "bench0_noslides"):
+        # an FP32 rounding artefact of the reference's Fresnel/Snell chain
+        # (CUDA/CUDAISMLMC.h:79-96, 71-76) leaves a packet that enters a slide
+        # from tissue at |mu_z| < ~2.4e-4 totally reflected at both slide
+        # faces; its loop (CUDAISMLMC.h:178-262) ends only when curand_uniform
+        # returns exactly 1.0f, about once in 2^25 draws, so a call on a stack
+        # with slides runs for an unbounded time
+        print(json.dumps(dict(base, unavailable=(
+            "the reference's CUDA kernel is timed only on stacks without slides: a packet "
+            "entering a slide near grazing is trapped by FP32 total reflection at both faces and "
+            "loops until curand returns exactly 1.0f (~2^25 draws)"))), flush=True)
+        return
+    try:
+        from oracle import build_ref
+        exe = build_ref.build_refcuda()
+    except RuntimeError as e:
+        print(json.dumps(dict(base, unavailable="reference CUDA build failed: " +
+                              str(e).splitlines()[0])), flush=True)
+        return
+    if not exe:
+        print(json.dumps(dict(base, unavailable="the reference's CUDA sources were not staged into "
+                              "oracle/_ref/src (oracle/build_ref.py stage())")), flush=True)
+        return
+    layers = workload_layers(st)
+    sp = workload_spheres()
+    per_call = min(REFCUDA_PACKETS_PER_CALL, args.packets)
+    calls_per_step = max(1, math.ceil(args.packets / per_call))
+    calls = calls_per_step * args.steps
+
+    def arr(xs):
+        return " ".join(f"{x:.9g}" for x in xs)
+
+    cmd = [exe, "--layers", str(len(layers)), "-n", arr(l.n for l in layers),
+           "-g", arr(l.g for l in layers), "-t", arr(l.d for l in layers),
+           "--mua", arr(l.mua for l in layers), "--mus", arr(l.mus for l in layers),
+           "--Rsphere", arr((sp.R_pw, sp.R_fs, sp.R_fp, sp.R_fd)),
+           "--Tsphere", arr((sp.T_pw, sp.T_fs, sp.T_fp, sp.T_fd)),
+           "--packets", str(per_call), "--calls", str(calls)]
+    with ClockSampler(0) as clk:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=1800)
+    if r.returncode != 0:
+        raise RuntimeError(f"refcuda_bench failed ({r.returncode}): {r.stderr[-2000:]}")
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    packets = per_call * calls
+    kern = sum(out["kernel_s"])
+    e2e = sum(out["e2e_s"])
+    value = packets / kern
+    line = dict(base, value=value, n_gpus=1, steps=args.steps, warmup=1,
+                ms_per_step=1000 * kern / args.steps, higher_is_better=True, scaling="weak",
+                vs_baseline=None, dtype="f32", data="synthetic",
+                e2e={"value": packets / e2e, "unit": "photons/s",
+                     "api": "the reference's ISMLMC() (CUDA/CUDAISMLMC.h:656-755), host clock"},
+                clocks=clk.summary(),
+                result={"packets_per_call": per_call, "calls_per_step": calls_per_step,
+                        "kernel_mean": out["kernel_mean"], "e2e_mean": out["e2e_mean"],
+                        "registers": out["registers"], "launch": f"{out['blocks']} x {out['threads']}",
+                        "kernel_s": out["kernel_s"], "e2e_s": out["e2e_s"]},
+                note="value: the reference's kernel alone (CUDA events, device-resident arrays, "
+                     "its own launch shape); warm-up: one untimed ISMLMC() call that initialises "
+                     "the curand states.  Its roulette never lets a packet survive "
+                     "(CUDAISMLMC.h:275: integer 1/m = 0) and its tallies are float atomics.")
     print(json.dumps(line), flush=True)
 
 
@@ -345,7 +457,8 @@ def run_gpu(args, rank, world, dist):
     torch.cuda.set_device(dev)
     eng = Engine(dev)
     n = args.packets
-    inst = workload_instance(n, offset=rank * n)
+    st = args.stack
+    inst = workload_instance(n, offset=rank * n, stack=st)
     # the autotuner picks block size and queue chunking on short trial launches
     # of the same workload (kept in the context for every launch below)
     tuned = eng.autotune([inst])
@@ -398,10 +511,24 @@ def run_gpu(args, rank, world, dist):
     barrier()
     e2e_time = sum(e2e_times)
 
+    merge = None
     if dist is not None:
         t = torch.tensor([dev_time, e2e_time], dtype=torch.float64, device=f"cuda:{dev}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dev_time, e2e_time = float(t[0]), float(t[1])
+        # the one data exchange of a sharded run: the ranks' integer tallies are
+        # summed into the result of the whole packet range [0, world n) ...
+        from ismc_gb300 import distributed as D
+        from ismc_gb300 import tally_to_result
+        merged = D.allreduce_tallies([tally])[0]
+        res = tally_to_result(merged)
+        # ... and, at a reduced size, that sum equals one process's run of the
+        # same range bit for bit
+        check_n = min(n * world, 2_000_000)
+        _, same = D.sharded_run_check(lambda x: eng.run_batch_raw([x])[0],
+                                      workload_instance(check_n, stack=st), rank, world)
+        merge = {"merged_packets": int(merged.n), "check_packets": check_n,
+                 "sharded_equals_single_process": same}
     if rank != 0:
         return
     total_packets = n * args.steps * world
@@ -409,6 +536,7 @@ def run_gpu(args, rank, world, dist):
     e2e = total_packets / e2e_time
     steps_per_packet = tally.steps / n
     events_per_packet = tally.events / n
+    trapped = tally.trapped
     clocks = clk.summary()
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     prof = load_roofline_profile()
@@ -417,7 +545,7 @@ def run_gpu(args, rank, world, dist):
             "note": "issue-rate roofline: SMs x SM clock x 128 lanes vs photon-steps/s x "
                     "thread-instructions per step (ncu, profiles/)"}
     steps_per_s = tally.steps * world * args.steps / dev_time
-    if prof and clocks.get("sm_mhz"):
+    if prof and clocks.get("sm_mhz") and st == "bench1":
         ips = float(prof["thread_inst_per_step"])
         peak = sms * clocks["sm_mhz"] * 1e6 * 128 / 1e9
         ach = steps_per_s * ips / 1e9
@@ -426,6 +554,16 @@ def run_gpu(args, rank, world, dist):
                     thread_inst_per_step=ips, steps_per_s=steps_per_s,
                     roofline_steps_per_s=peak * 1e9 / ips, clock="median SM clock under load",
                     source=os.path.relpath(ROOFLINE_FILE, ROOT))
+        # frac counts issue slots, whatever share of a warp's 32 lanes each
+        # instruction carries; these two count lanes that did work
+        if prof.get("thread_inst_executed_per_step"):
+            exe = float(prof["thread_inst_executed_per_step"])
+            roof.update(active_lane_frac=exe / ips,
+                        useful_frac=steps_per_s * exe / (peak * 1e9),
+                        thread_inst_executed_per_step=exe,
+                        useful_note="useful_frac = photon-steps/s x executed thread-instructions "
+                                    "per step / (SMs x clock x 128): the issue-rate fraction "
+                                    "with idle lanes of divergent instructions not counted")
     else:
         roof.update(steps_per_s=steps_per_s)
     # the HBM side, for completeness: DRAM bytes per launch (ncu) over the launch
@@ -435,13 +573,13 @@ def run_gpu(args, rank, world, dist):
         gbs = prof["dram_bytes_per_launch"] / (dev_time / args.steps) / 1e9
         roof["hbm"] = {"achieved_gbs": gbs, "peak_gbs": peaks["hbm_gbs"],
                        "frac": gbs / peaks["hbm_gbs"], "peak_source": "MEASURED_PEAKS.json (of measured)"}
-    cpu = cpu_baseline() if (world == 1 and not args.no_cpu_baseline) else None
+    cpu = cpu_baseline(stack=st) if (world == 1 and not args.no_cpu_baseline) else None
     line = {"metric": "photons/s", "value": value, "unit": "photons/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dev_time / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": dict(CONFIG, tune={"block_threads": int(tuned.block_threads),
-                                         "chunk": "sized on the device per batch"}),
+            "config": dict(workload_config(st, n), tune={"block_threads": int(tuned.block_threads),
+                                                         "chunk": "sized on the device per batch"}),
             "e2e": {"value": e2e, "unit": "photons/s", "h2d_bytes_per_step": C.sizeof(_abi.Instance),
                     "d2h_bytes_per_step": C.sizeof(_abi.Tally),
                     "api": "ismc_run_batch (host pointers)"},
@@ -450,8 +588,11 @@ def run_gpu(args, rank, world, dist):
             "roofline": roof,
             "cpu_baseline": cpu,
             "result": {"R_d": res.mean[1], "T_d": res.mean[3], "T_u": res.mean[4],
-                       "se": [res.se[1], res.se[3], res.se[4]],
-                       "steps_per_packet": steps_per_packet, "events_per_packet": events_per_packet}}
+                       "se": [res.se[1], res.se[3], res.se[4]], "packets": res.n,
+                       "steps_per_packet": steps_per_packet, "events_per_packet": events_per_packet,
+                       "trapped_packets": trapped}}
+    if merge is not None:
+        line["merge"] = merge
     print(json.dumps(line), flush=True)
 
 
@@ -530,10 +671,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--stack", choices=["bench1", "bench1_noslides", "bench0", "bench0_noslides"],
+                    default="bench1", help="layer stack of the forward workload (default: the "
+                                           "multilayer benchmark configuration)")
     ap.add_argument("--packets", type=int, default=PACKETS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["forward", "lookup", "tables", "surrogate", "solve",
-                                           "dropin", "train"],
+                                           "dropin", "train", "refcuda"],
                     default="forward")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="size factor for the secondary workloads (1 = full benchmark size)")
@@ -542,6 +686,11 @@ def main():
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.workload == "refcuda":
+        if args.impl != "reference":
+            ap.error("--workload refcuda is the reference CUDA arm: use --impl reference")
+        run_refcuda(args, rank)
+        return
     if args.workload != "forward":
         if rank == 0 and args.impl == "gpu":
             run_other_workload(args)

@@ -48,7 +48,8 @@ extern "C" {
 #define ISMC_ERR_STEP_LIMIT    (-3)   /* some packet exceeded the per-packet event cap */
 #define ISMC_ERR_NO_DEVICE     (-4)
 #define ISMC_ERR_ALLOC         (-5)
-#define ISMC_ERR_CAPACITY      (-6)   /* request larger than a fixed-capacity buffer */
+#define ISMC_ERR_CAPACITY      (-6)   /* request beyond a fixed capacity: a fixed-size
+                                         buffer, or ISMC_MAX_PACKETS per instance */
 #define ISMC_ERR_INTERNAL      (-7)
 
 /* propagation modes */
@@ -94,17 +95,31 @@ typedef struct ismc_spheres {
     double T_pw, T_fs, T_fp, T_fd, T_f, T_angle;
 } ismc_spheres;
 
+/*
+ * Largest packet count of one instance: 2^31.  Tallies are 64-bit sums of
+ * per-packet scores quantised to 2^-32 (ismc_tally), and a packet's scored
+ * weights add up to 1 on average (roulette_threshold * roulette_m <= 1 keeps
+ * every single score near that), so 2^31 packets use at most about half of
+ * the 2^64 range of any sum or sum of squares.  A larger simulation is split
+ * into instances with consecutive packet_offset ranges; their tallies add
+ * exactly, in wider than 64-bit arithmetic once the total passes 2^31
+ * packets.  Instances beyond the limit are refused with ISMC_ERR_CAPACITY
+ * instead of returning wrapped sums.
+ */
+#define ISMC_MAX_PACKETS 2147483648ull
+
 /* One simulation instance of a batch. */
 typedef struct ismc_instance {
     ismc_stack stack;
     ismc_spheres spheres;
-    uint64_t n_packets;       /* packets to launch */
+    uint64_t n_packets;       /* packets to launch, at most ISMC_MAX_PACKETS */
     uint64_t packet_offset;   /* id of the first packet (sharding / resume) */
     uint64_t seed;            /* Philox key */
     uint32_t stream;          /* Philox stream id (independent streams per seed) */
     uint32_t mode;            /* ISMC_MODE_* */
     float roulette_threshold; /* 1e-4 as in MLMC.py:86, 1e-3 as in ISMC.py:136 */
-    float roulette_m;         /* survival 1/m, weight *m (10 in the reference) */
+    float roulette_m;         /* survival 1/m, weight *m (10 in the reference);
+                                 m >= 1 and roulette_threshold * m <= 1 */
 } ismc_instance;
 
 /*
@@ -126,7 +141,8 @@ typedef struct ismc_tally {
                                  near-grazing entry, ~1e-7 per entry): their weight
                                  is dropped instead of bouncing forever */
     uint32_t scale_log2;
-    int32_t status;           /* ISMC_OK or ISMC_ERR_STEP_LIMIT */
+    int32_t status;           /* ISMC_OK, ISMC_ERR_STEP_LIMIT, or (instance not run, n = 0)
+                                 ISMC_ERR_INVALID_ARG / ISMC_ERR_CAPACITY */
     float analytic_specular;  /* deterministic specular reflectance of the stack (see ismc_run) */
     float analytic_ballistic; /* deterministic unscattered transmittance (normal incidence) */
 } ismc_tally;
@@ -197,8 +213,10 @@ int ismc_run_batch_device(ismc_ctx* ctx, const ismc_instance* d_inst, uint32_t n
  * kept by every GPU that loads the library until the process exits).
  *   - Needs no context; runs on the calling thread's current device and on
  *     `stream` as given (NULL = legacy default stream).
- *   - The first call on a device looks up the array's device address; make
- *     that first call before any stream capture.
+ *   - The array has one address per CUDA context.  The first call in each
+ *     context (the device's primary context, a driver-API context the caller
+ *     made current, or the new primary context after cudaDeviceReset) looks
+ *     that address up; make that first call before any stream capture.
  *   - n_inst > ISMC_NOALLOC_MAX_INST returns ISMC_ERR_CAPACITY (message in
  *     ismc_last_error(NULL, ...)).
  *   - All calls share the one array: calls that overlap on the GPU (different
@@ -209,6 +227,17 @@ int ismc_run_batch_device(ismc_ctx* ctx, const ismc_instance* d_inst, uint32_t n
 #define ISMC_NOALLOC_MAX_INST 1024
 int ismc_run_batch_noalloc(const ismc_instance* d_inst, uint32_t n_inst, const ismc_tune* tune,
                            ismc_tally* d_out, void* stream);
+
+/*
+ * Host-side check of a batch, no GPU needed: the checks ismc_run_batch makes
+ * before it launches anything (layer parameters, mode, roulette, and
+ * n_packets <= ISMC_MAX_PACKETS).  status (n_inst entries, may be NULL)
+ * receives ISMC_OK, ISMC_ERR_INVALID_ARG or ISMC_ERR_CAPACITY per instance;
+ * the return value is the first instance's error, its text in
+ * ismc_last_error(NULL, ...).  The device-pointer entry points make the same
+ * checks on the GPU and report them in each tally's status.
+ */
+int ismc_validate(const ismc_instance* inst, uint32_t n_inst, int32_t* status);
 
 /* Choose block size / chunk size for a representative batch by timing short
  * trial launches; the choice is stored in the context and returned in *out. */
@@ -293,6 +322,12 @@ int ismc_mlp_sync(ismc_mlp* m);
 int ismc_mlp_gemm_test(ismc_mlp* m, const void* d_a, const void* d_b, float* d_d, int M, int N,
                        int K, int splits);   /* D = A B^T, bf16 K-major operands, for tests */
 int ismc_mlp_last_error(const ismc_mlp* m, char* buf, size_t n);
+/* Polls each tensor-core pipeline wait makes before it gives up (default
+ * 4194304, seconds at most).  A wait that runs out records an error that the
+ * next synchronising call returns as ISMC_ERR_INTERNAL; the block first lets
+ * its own tile copies and MMAs finish and frees its TMEM, so the context stays
+ * usable.  0 makes every first wait give up at once: for tests of that path. */
+int ismc_mlp_set_wait_limit(ismc_mlp* m, uint32_t polls);
 
 /* ------------------------------------------------------------------------
  * Lookup-table inversion (Lookup/lookup.py:301-489).  Host arrays in and out

@@ -81,14 +81,16 @@ SIZEOF_INDEX = {0: Stack, 1: Spheres, 2: Instance, 3: Tally, 4: Tune, 5: SolveRe
 # every symbol include/ismc.h declares
 EXPORTS = ("ismc_version", "ismc_init", "ismc_destroy", "ismc_run", "ismc_run_batch",
            "ismc_run_batch_device", "ismc_autotune", "ismc_last_error", "ismc_sizeof",
-           "ismc_solve_batch", "ismc_praxis", "ismc_run_batch_noalloc",
+           "ismc_solve_batch", "ismc_praxis", "ismc_run_batch_noalloc", "ismc_validate",
            "ismc_mlp_create", "ismc_mlp_destroy", "ismc_mlp_nparam", "ismc_mlp_get_params",
            "ismc_mlp_set_params", "ismc_mlp_forward", "ismc_mlp_grad", "ismc_mlp_train_step",
            "ismc_mlp_sync", "ismc_mlp_gemm_test", "ismc_mlp_last_error", "ismc_mlp_train_epoch",
+           "ismc_mlp_set_wait_limit",
            "ismc_table_interp", "ismc_table_interp_cubic", "ismc_table_uncertainty",
            "ismc_table_lookup")
 
-NOALLOC_MAX_INST = 1024
+NOALLOC_MAX_INST = 1024          # ISMC_NOALLOC_MAX_INST
+MAX_PACKETS = 1 << 31            # ISMC_MAX_PACKETS: packets of one instance
 
 
 def declare(lib):
@@ -117,6 +119,8 @@ def declare(lib):
     lib.ismc_praxis.restype = C.c_int
     lib.ismc_praxis.argtypes = [OBJECTIVE, C.c_void_p, C.c_int, P(C.c_double), C.c_double,
                                 C.c_double, C.c_int, P(C.c_double), P(C.c_int)]
+    lib.ismc_validate.restype = C.c_int
+    lib.ismc_validate.argtypes = [P(Instance), C.c_uint32, P(C.c_int32)]
     lib.ismc_run_batch_noalloc.restype = C.c_int
     lib.ismc_run_batch_noalloc.argtypes = [C.c_void_p, C.c_uint32, P(Tune), C.c_void_p, C.c_void_p]
     V, F = C.c_void_p, P(C.c_float)
@@ -142,6 +146,8 @@ def declare(lib):
     lib.ismc_mlp_sync.argtypes = [V]
     lib.ismc_mlp_gemm_test.restype = C.c_int
     lib.ismc_mlp_gemm_test.argtypes = [V, V, V, V, C.c_int, C.c_int, C.c_int, C.c_int]
+    lib.ismc_mlp_set_wait_limit.restype = C.c_int
+    lib.ismc_mlp_set_wait_limit.argtypes = [V, C.c_uint32]
     lib.ismc_mlp_last_error.restype = C.c_int
     lib.ismc_mlp_last_error.argtypes = [V, C.c_char_p, C.c_size_t]
     D = P(C.c_double)

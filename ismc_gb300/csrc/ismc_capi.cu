@@ -244,26 +244,65 @@ static int enqueue_pipeline(ismc_ctx* ctx, const ismc_instance* d_in, uint32_t n
     return 0;
 }
 
-static int check_instances(ismc_ctx* ctx, const ismc_instance* in, uint32_t n) {
-    for (uint32_t i = 0; i < n; ++i) {
-        const ismc_stack& S = in[i].stack;
-        if (S.L < 1 || S.L > ISMC_MAXL)
-            return set_err(ctx, ISMC_ERR_INVALID_ARG, "instance %u: L=%u outside [1,%d]", i, S.L, ISMC_MAXL);
-        if (in[i].mode > ISMC_MODE_PHYSICAL)
-            return set_err(ctx, ISMC_ERR_INVALID_ARG, "instance %u: unknown mode %u", i, in[i].mode);
-        for (uint32_t l = 0; l < S.L; ++l) {
-            if (!(S.n[l] > 0.0f) || !(S.d[l] > 0.0f) || !(S.mua[l] >= 0.0f) || !(S.mus[l] >= 0.0f) ||
-                !(S.mut[l] >= 0.0f) || !(S.g[l] >= -1.0f && S.g[l] <= 1.0f) ||
-                (S.mus[l] != 0.0f && !(S.mut[l] > 0.0f)))
-                return set_err(ctx, ISMC_ERR_INVALID_ARG,
-                               "instance %u layer %u: need n>0, d>0, mua,mus,mut>=0, |g|<=1, mut>0 "
-                               "when mus>0 (got n=%g d=%g mua=%g mus=%g mut=%g g=%g)",
-                               i, l, S.n[l], S.d[l], S.mua[l], S.mus[l], S.mut[l], S.g[l]);
+// One instance's host-side check; the message goes to buf.  The prepare kernel
+// (ismc_kernels.cu) makes the same checks on the device.
+static int check_one(const ismc_instance& I, uint32_t i, char* buf, size_t nbuf) {
+    const ismc_stack& S = I.stack;
+    if (S.L < 1 || S.L > ISMC_MAXL) {
+        snprintf(buf, nbuf, "instance %u: L=%u outside [1,%d]", i, S.L, ISMC_MAXL);
+        return ISMC_ERR_INVALID_ARG;
+    }
+    if (I.mode > ISMC_MODE_PHYSICAL) {
+        snprintf(buf, nbuf, "instance %u: unknown mode %u", i, I.mode);
+        return ISMC_ERR_INVALID_ARG;
+    }
+    for (uint32_t l = 0; l < S.L; ++l) {
+        if (!(S.n[l] > 0.0f) || !(S.d[l] > 0.0f) || !(S.mua[l] >= 0.0f) || !(S.mus[l] >= 0.0f) ||
+            !(S.mut[l] >= 0.0f) || !(S.g[l] >= -1.0f && S.g[l] <= 1.0f) ||
+            (S.mus[l] != 0.0f && !(S.mut[l] > 0.0f))) {
+            snprintf(buf, nbuf,
+                     "instance %u layer %u: need n>0, d>0, mua,mus,mut>=0, |g|<=1, mut>0 "
+                     "when mus>0 (got n=%g d=%g mua=%g mus=%g mut=%g g=%g)",
+                     i, l, S.n[l], S.d[l], S.mua[l], S.mus[l], S.mut[l], S.g[l]);
+            return ISMC_ERR_INVALID_ARG;
         }
-        if (!(in[i].roulette_m >= 1.0f))
-            return set_err(ctx, ISMC_ERR_INVALID_ARG, "instance %u: roulette_m must be >= 1", i);
+    }
+    if (!(I.roulette_m >= 1.0f) || !(I.roulette_threshold >= 0.0f) ||
+        !(I.roulette_threshold * I.roulette_m <= 1.0f)) {
+        snprintf(buf, nbuf, "instance %u: roulette needs m >= 1 and 0 <= threshold * m <= 1 "
+                            "(got threshold %g, m %g)", i, I.roulette_threshold, I.roulette_m);
+        return ISMC_ERR_INVALID_ARG;
+    }
+    if (I.n_packets > ISMC_MAX_PACKETS) {
+        snprintf(buf, nbuf, "instance %u: %llu packets exceed ISMC_MAX_PACKETS (2^31) of one "
+                            "instance, beyond which 64-bit tallies could wrap; split it into "
+                            "instances with consecutive packet_offset ranges",
+                 i, (unsigned long long)I.n_packets);
+        return ISMC_ERR_CAPACITY;
     }
     return 0;
+}
+
+static int check_instances(ismc_ctx* ctx, const ismc_instance* in, uint32_t n) {
+    char msg[400];
+    for (uint32_t i = 0; i < n; ++i) {
+        const int rc = check_one(in[i], i, msg, sizeof msg);
+        if (rc) return set_err(ctx, rc, "%s", msg);
+    }
+    return 0;
+}
+
+extern "C" int ismc_validate(const ismc_instance* inst, uint32_t n_inst, int32_t* status) {
+    if (!inst && n_inst)
+        return set_err(nullptr, ISMC_ERR_INVALID_ARG, "validate: inst is NULL");
+    char msg[400];
+    int first = 0;
+    for (uint32_t i = 0; i < n_inst; ++i) {
+        const int rc = check_one(inst[i], i, msg, sizeof msg);
+        if (status) status[i] = rc;
+        if (rc && !first) first = set_err(nullptr, rc, "%s", msg);
+    }
+    return first;
 }
 
 extern "C" int ismc_run_batch_device(ismc_ctx* ctx, const ismc_instance* d_inst, uint32_t n_inst,

@@ -126,8 +126,12 @@ __global__ void ismc_prepare_kernel(const ismc_instance* __restrict__ in, uint32
         cR = sqrt(1.0 - fpR);
         cT = sqrt(1.0 - fpT);
         ok = ok && ismc_finite(pR) && ismc_finite(pT) && ismc_finite(cR) && ismc_finite(cT) &&
-             I.roulette_m >= 1.0f && ismc_finite(I.roulette_threshold);
+             I.roulette_m >= 1.0f && I.roulette_threshold >= 0.0f &&
+             I.roulette_threshold * I.roulette_m <= 1.0f;
     }
+    // 64-bit tallies at 2^-32 per unit weight: at most 2^31 packets (ismc.h)
+    const bool fits = I.n_packets <= ISMC_MAX_PACKETS;
+    const bool run = ok && fits;
     // ---------------------------------------------------------------- header
     D.L = L;
     D.mode = I.mode;
@@ -233,14 +237,14 @@ __global__ void ismc_prepare_kernel(const ismc_instance* __restrict__ in, uint32
 
     // ---------------------------------------------------------------- tally / queue
     ismc_tally& T = tally[i];
-    T.n = ok ? I.n_packets : 0ull;
+    T.n = run ? I.n_packets : 0ull;
     for (int k = 0; k < 5; ++k) { T.sum[k] = 0ull; T.sumsq[k] = 0ull; }
     T.steps = T.events = T.reincidences = T.capped = T.trapped = 0ull;
     T.scale_log2 = 32u;
-    T.status = ok ? ISMC_OK : ISMC_ERR_INVALID_ARG;
+    T.status = !ok ? ISMC_ERR_INVALID_ARG : (fits ? ISMC_OK : ISMC_ERR_CAPACITY);
     T.analytic_specular = spec;
     T.analytic_ballistic = ball;
-    const uint64_t cnt = ok ? I.n_packets : 0ull;
+    const uint64_t cnt = run ? I.n_packets : 0ull;
     range[i].offset = I.packet_offset;
     range[i].count = cnt;
 }

@@ -48,7 +48,12 @@ namespace {
 
 constexpr int BM = 128;           // rows per tile (tcgen05 M)
 constexpr int BK = 64;            // K per stage: 64 bf16 = one 128-byte swizzle row
-constexpr uint32_t WAIT_LIMIT = 1u << 22;   // polls of a bounded try_wait: seconds at most
+// polls of a bounded try_wait: seconds at most.  The pipeline waits use the
+// context's limit (this default, or a test's setting); the drain after a
+// timed-out wait, which lets the block's own copies and MMAs finish before it
+// releases its shared memory and TMEM, always uses this one.
+constexpr uint32_t WAIT_LIMIT = 1u << 22;
+constexpr uint32_t DRAIN_LIMIT = 1u << 22;
 // threads of a GEMM CTA: warp 0 allocates TMEM and thread 0 drives TMA and the
 // MMAs; in the epilogue warps w and w + 4 read TMEM lanes 32 (w % 4) .. + 31,
 // each for half of the tile's columns
@@ -88,7 +93,8 @@ __host__ __device__ constexpr int gemm_stages() { return BN <= 64 ? 4 : 2; }
 template <int BN, int MODE>
 __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(const __grid_constant__ CUtensorMap tA,
                                                                  const __grid_constant__ CUtensorMap tB,
-                                                                 int k_chunks, Epi e, int* err) {
+                                                                 int k_chunks, Epi e, int* err,
+                                                                 uint32_t wait_limit) {
     static_assert(BN >= 16 && BN <= 256 && BN % 16 == 0, "tile N");
     constexpr int S = gemm_stages<BN>();
     constexpr uint32_t A_BYTES = BM * BK * 2;
@@ -168,11 +174,18 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(const __grid
 
     if (threadIdx.x == 0) {
         const uint32_t sa0 = umma::smem_u32(smem), sb0 = sa0 + A_BYTES;
+        // fills requested / consumed per stage, and whether any MMA was issued:
+        // what a timed-out pipeline still has in flight
+        int nfill[S], nused[S];
+#pragma unroll
+        for (int s = 0; s < S; ++s) nfill[s] = nused[s] = 0;
+        bool mma_issued = false;
         auto load = [&](int kc, int s) {
             const uint32_t bar = umma::smem_u32(bars + s);
             umma::mbar_expect_tx(bar, STAGE);
             umma::tma_load_2d(sa0 + s * STAGE, &tA, (kc0 + kc) * BK, m0, bar);
             umma::tma_load_2d(sb0 + s * STAGE, &tB, (kc0 + kc) * BK, n0, bar);
+            ++nfill[s];
         };
         bool ok = true;
         // chunk j lives in stage j % S and is that stage's (j / S)-th fill;
@@ -180,36 +193,58 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(const __grid
         for (int kc = 0; kc < S && kc < k_chunks; ++kc) load(kc, kc);
         for (int kc = 0; kc < k_chunks && ok; ++kc) {
             const int s = kc % S;
-            if (!umma::mbar_wait(umma::smem_u32(bars + s), (kc / S) & 1, WAIT_LIMIT)) {
+            if (!umma::mbar_wait(umma::smem_u32(bars + s), (kc / S) & 1, wait_limit)) {
                 ok = false;
                 break;
             }
+            ++nused[s];
             umma::fence_after_sync();
             const uint64_t da = umma::desc_sw128(sa0 + s * STAGE);
             const uint64_t db = umma::desc_sw128(sb0 + s * STAGE);
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk)     // 16 bf16 = 32 B per MMA: +2 in the address field
                 umma::mma_bf16(tmem, da + 2 * kk, db + 2 * kk, IDESC, (kc | kk) != 0);
+            mma_issued = true;
             umma::mma_commit(umma::smem_u32(bars + S + s));
             // refill the stage the previous chunk used, once its MMAs are done
             const int pk = kc - 1, nk = pk + S;
             if (pk >= 0 && nk < k_chunks) {
                 const int ps = pk % S;
-                if (!umma::mbar_wait(umma::smem_u32(bars + S + ps), (pk / S) & 1, WAIT_LIMIT)) {
+                if (!umma::mbar_wait(umma::smem_u32(bars + S + ps), (pk / S) & 1, wait_limit)) {
                     ok = false;
                     break;
                 }
                 load(nk, ps);
             }
         }
-        if (ok) umma::mma_commit(umma::smem_u32(bars + 2 * S));
-        else *sfail = 1;
+        if (ok) {
+            umma::mma_commit(umma::smem_u32(bars + 2 * S));
+        } else {
+            // drain before the block gives up its shared memory and TMEM: every
+            // requested tile lands (the last fill of each stage not yet
+            // consumed) and every issued MMA completes (a commit tracks all of
+            // this thread's earlier MMAs)
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+                if (nfill[s] > nused[s])
+                    umma::mbar_wait(umma::smem_u32(bars + s), (nfill[s] - 1) & 1, DRAIN_LIMIT);
+            if (mma_issued) {
+                umma::mma_commit(umma::smem_u32(bars + 2 * S));
+                umma::mbar_wait(umma::smem_u32(bars + 2 * S), 0, DRAIN_LIMIT);
+            }
+            *sfail = 1;
+        }
     }
     __syncthreads();
-    bool ok = *sfail == 0;
-    if (ok) ok = umma::mbar_wait(umma::smem_u32(bars + 2 * S), 0, WAIT_LIMIT);
+    const bool committed = *sfail == 0;      // the final commit was issued
+    bool ok = committed;
+    if (ok) ok = umma::mbar_wait(umma::smem_u32(bars + 2 * S), 0, wait_limit);
     // one verdict for the block: the epilogue below synchronises the block
     ok = __syncthreads_and(ok) != 0;
+    // a block that gave up waiting for its MMAs lets them finish before TMEM
+    // is released
+    if (!ok && committed && threadIdx.x == 0)
+        umma::mbar_wait(umma::smem_u32(bars + 2 * S), 0, DRAIN_LIMIT);
     // the operands are consumed: the next product may start its set-up
     umma::grid_dep_launch();
     if (!ok) {
@@ -536,6 +571,7 @@ struct ismc_mlp {
     EncodeTiledFn encode = nullptr;
     int* d_err = nullptr;
     float* d_loss = nullptr;
+    uint32_t wait_limit = WAIT_LIMIT;   // polls of each pipeline wait (tests lower it)
     // parameters: fp32 master, grads, Adam moments (one flat buffer each)
     size_t nparam = 0;
     size_t off_w[4], off_b[4];
@@ -661,7 +697,7 @@ static int launch_gemm(ismc_mlp* m, const void* A, int M, int K, const void* B, 
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cudaError_t err = cudaLaunchKernelEx(&cfg, umma_gemm_kernel<BN, MODE>, ta, tb, K / BK / splits, e,
-                                         m->d_err);
+                                         m->d_err, m->wait_limit);
     if (err == cudaSuccess) err = cudaGetLastError();
     return err == cudaSuccess ? 0 : mlp_err(m, ISMC_ERR_CUDA, "gemm launch", err);
 }
@@ -894,7 +930,18 @@ static int check_err(ismc_mlp* m) {
     int h = 0;
     MCK(cudaMemcpyAsync(&h, m->d_err, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
     MCK(cudaStreamSynchronize(m->stream));
-    if (h) return mlp_err(m, ISMC_ERR_INTERNAL, "tensor-core pipeline wait timed out");
+    if (h) {
+        // reported once: the next call starts with a clear flag
+        MCK(cudaMemsetAsync(m->d_err, 0, sizeof(int), m->stream));
+        MCK(cudaStreamSynchronize(m->stream));
+        return mlp_err(m, ISMC_ERR_INTERNAL, "tensor-core pipeline wait timed out");
+    }
+    return 0;
+}
+
+extern "C" int ismc_mlp_set_wait_limit(ismc_mlp* m, uint32_t polls) {
+    if (!m) return ISMC_ERR_INVALID_ARG;
+    m->wait_limit = polls;
     return 0;
 }
 

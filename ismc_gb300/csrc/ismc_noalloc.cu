@@ -13,6 +13,8 @@
 // here in one file-scope __device__ array of fixed size, sized for at most
 // ISMC_NOALLOC_MAX_INST instances (about 1.2 MB).  Every GPU that loads the
 // library keeps that array until the process exits.
+#include <cuda.h>          // CUcontext / CUresult types only; the driver calls go
+                           // through cudaGetDriverEntryPointByVersion, no -lcuda
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <mutex>
@@ -36,38 +38,92 @@ static __device__ __align__(256) unsigned char ismc_noalloc_scratch[sizeof(Noall
 
 namespace {
 
-constexpr int kMaxDevices = 64;
+// A __device__ array has one address per CUDA context that loaded the
+// library's module, not per device: a host application may make its own
+// driver-API context current, and cudaDeviceReset replaces the primary
+// context (and the array's address) with a new one.  The looked-up address is
+// therefore cached per context, keyed by the context's process-unique ID.
+constexpr int kMaxContexts = 64;
 
-struct DeviceSetup {
-    bool done = false;
+struct ContextSetup {
+    unsigned long long ctx_id = 0;
     int sms = 0;
     NoallocScratch* scratch = nullptr;   // device address of ismc_noalloc_scratch
 };
 
-std::mutex g_setup_mu;
-DeviceSetup g_setup[kMaxDevices];
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
 
-// Once per device, with that device current: look up the array's device
-// address and the SM count.
-int device_setup(int dev, DeviceSetup** out) {
+std::mutex g_setup_mu;
+ContextSetup g_setup[kMaxContexts];
+int g_n_setup = 0, g_next_slot = 0;
+PfnCtxGetCurrent g_ctx_get_current = nullptr;
+PfnCtxGetId g_ctx_get_id = nullptr;
+
+int resolve_driver_calls() {
+    if (g_ctx_get_current && g_ctx_get_id) return 0;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000,
+                                                      cudaEnableDefault, &q1);
+    cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000,
+                                                      cudaEnableDefault, &q2);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+        q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+        return ismc_lib_error(ISMC_ERR_CUDA, "run_batch_noalloc: cuCtxGetCurrent / cuCtxGetId "
+                                             "unavailable from the driver");
+    g_ctx_get_current = reinterpret_cast<PfnCtxGetCurrent>(f1);
+    g_ctx_get_id = reinterpret_cast<PfnCtxGetId>(f2);
+    return 0;
+}
+
+// Once per CUDA context, with that context current: look up the array's
+// device address in it and the device's SM count.  A thread with no current
+// context gets the device's primary context, which the runtime's first call
+// (cudaGetSymbolAddress) creates and makes current.
+int context_setup(int dev, ContextSetup* out) {
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    DeviceSetup& d = g_setup[dev];
-    if (!d.done) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, ismc_noalloc_scratch);
+    int rc = resolve_driver_calls();
+    if (rc) return rc;
+    CUcontext c = nullptr;
+    if (g_ctx_get_current(&c) != CUDA_SUCCESS)
+        return ismc_lib_error(ISMC_ERR_CUDA, "run_batch_noalloc: cuCtxGetCurrent failed");
+    void* p = nullptr;
+    if (!c) {
+        const cudaError_t e = cudaGetSymbolAddress(&p, ismc_noalloc_scratch);
         if (e != cudaSuccess)
             return ismc_lib_error(ISMC_ERR_CUDA, "run_batch_noalloc: cudaGetSymbolAddress failed: %s",
                                   cudaGetErrorString(e));
-        int sms = 0;
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess || sms <= 0)
-            return ismc_lib_error(ISMC_ERR_CUDA, "run_batch_noalloc: SM count query failed: %s",
-                                  cudaGetErrorString(e));
-        d.scratch = static_cast<NoallocScratch*>(p);
-        d.sms = sms;
-        d.done = true;
+        if (g_ctx_get_current(&c) != CUDA_SUCCESS || !c)
+            return ismc_lib_error(ISMC_ERR_CUDA, "run_batch_noalloc: no current CUDA context");
     }
-    *out = &d;
+    unsigned long long id = 0;
+    if (g_ctx_get_id(c, &id) != CUDA_SUCCESS)
+        return ismc_lib_error(ISMC_ERR_CUDA, "run_batch_noalloc: cuCtxGetId failed");
+    for (int k = 0; k < g_n_setup; ++k) {
+        if (g_setup[k].ctx_id == id) {
+            *out = g_setup[k];   // a copy: the table entry may be reused later
+            return 0;
+        }
+    }
+    cudaError_t e = cudaGetSymbolAddress(&p, ismc_noalloc_scratch);
+    if (e != cudaSuccess)
+        return ismc_lib_error(ISMC_ERR_CUDA, "run_batch_noalloc: cudaGetSymbolAddress failed: %s",
+                              cudaGetErrorString(e));
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess || sms <= 0)
+        return ismc_lib_error(ISMC_ERR_CUDA, "run_batch_noalloc: SM count query failed: %s",
+                              cudaGetErrorString(e));
+    // a bounded table: past kMaxContexts contexts (each cudaDeviceReset makes
+    // a new one) the oldest entry is reused
+    const int slot = g_n_setup < kMaxContexts ? g_n_setup++ : g_next_slot;
+    if (g_n_setup == kMaxContexts) g_next_slot = (slot + 1) % kMaxContexts;
+    g_setup[slot].ctx_id = id;
+    g_setup[slot].scratch = static_cast<NoallocScratch*>(p);
+    g_setup[slot].sms = sms;
+    *out = g_setup[slot];
     return 0;
 }
 
@@ -87,11 +143,10 @@ extern "C" int ismc_run_batch_noalloc(const ismc_instance* d_inst, uint32_t n_in
     if (e != cudaSuccess)
         return ismc_lib_error(ISMC_ERR_NO_DEVICE, "run_batch_noalloc: no current CUDA device: %s",
                               cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices)
-        return ismc_lib_error(ISMC_ERR_INVALID_ARG, "run_batch_noalloc: device %d not supported", dev);
-    DeviceSetup* d = nullptr;
-    int rc = device_setup(dev, &d);
+    ContextSetup setup;
+    int rc = context_setup(dev, &setup);
     if (rc) return rc;
+    const ContextSetup* d = &setup;
 
     const uint32_t threads = (tune && tune->block_threads) ? tune->block_threads : 256u;
     if (threads % 32 || threads > 512)

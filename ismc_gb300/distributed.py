@@ -59,3 +59,20 @@ def allreduce_tallies(tallies, group=None):
         m.status = int(status[i])
         out.append(m)
     return out
+
+
+def tallies_equal(a, b):
+    """Bit equality of two tallies' integer fields and status."""
+    return bytes(a)[:8 * SUM_WORDS] == bytes(b)[:8 * SUM_WORDS] and int(a.status) == int(b.status)
+
+
+def sharded_run_check(run, inst, rank, world, group=None):
+    """Simulate `inst` sharded over the process group -- each rank runs its
+    packet range with `run` (a callable taking one instance and returning its
+    ismc_tally) -- and merge the shards with allreduce_tallies.  Rank 0 then
+    runs the whole range alone and compares.  Returns (merged tally, True or
+    False on rank 0 / None elsewhere)."""
+    mine = run(shard_instance(inst, rank, world))
+    merged = allreduce_tallies([mine], group)[0]
+    same = tallies_equal(merged, run(inst)) if rank == 0 else None
+    return merged, same

@@ -1,23 +1,72 @@
-"""Compile parts of the reference from its own sources, in place, into
-oracle/_ref/ (git-ignored).  ORACLE: test infrastructure only.
+"""Build parts of the reference from its own sources into oracle/_ref/
+(git-ignored).  ORACLE / baseline infrastructure only.
 
-  oracle/_ref/libpraxis_ref.so   CUDA/praxis.cpp (+ oracle/praxis_ref_shim.cpp)
+  oracle/_ref/libpraxis_ref.so   CUDA/praxis.cpp (+ oracle/praxis_ref_shim.cpp),
+                                 compiled in place where the reference checkout
+                                 exists; tests compare the project's PRAXIS with it
+  oracle/_ref/src/CUDAISMLMC.h   a byte-for-byte copy of the reference's CUDA
+                                 forward model (CUDA/CUDAISMLMC.h), staged here
+                                 so that it travels with the working tree to the
+                                 GPU machine, where the reference checkout is
+                                 absent.  It is never committed (oracle/_ref/ is
+                                 git-ignored) and never edited.
+  oracle/_ref/refcuda_bench      oracle/refcuda_bench.cu, the project's timing
+                                 harness, compiled against the staged header
+                                 for sm_103a (build_refcuda(), on the GPU
+                                 machine, on demand)
 
-Runs only where the reference checkout exists (this needs REFERENCE_DIR or the
-default checkout path); elsewhere it does nothing and the tests that use its
-output skip.  The reference's CUDA programs are not built here: their binaries
-would not run on the Arm GPU machine and their sources are not present there.
+The reference checkout is found through REFERENCE_DIR, else at its usual
+location in the build container; where neither exists, the in-place builds are
+skipped and whatever was staged earlier is used.
 """
+import hashlib
 import os
+import shutil
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF = os.environ.get("REFERENCE_DIR", "/root/reference")
+SRC = os.path.join(OUT, "src")
+DEFAULT_REFERENCE_DIR = "/root/reference"
+# the reference's CUDA forward model: kernel CUDAISMLMC (CUDAISMLMC.h:316-654)
+# and its host wrapper ISMLMC() (CUDAISMLMC.h:656-755)
+STAGED = ("CUDA/CUDAISMLMC.h",)
+HARNESS = os.path.join(HERE, "refcuda_bench.cu")
+REFCUDA_BIN = os.path.join(OUT, "refcuda_bench")
 
 
-def build():
-    src = os.path.join(REF, "CUDA", "praxis.cpp")
+def reference_dir():
+    """The reference checkout, or None where it is absent."""
+    d = os.environ.get("REFERENCE_DIR", DEFAULT_REFERENCE_DIR)
+    return d if os.path.isdir(d) else None
+
+
+def _sha(path):
+    with open(path, "rb") as fh:
+        return hashlib.sha256(fh.read()).hexdigest()
+
+
+def stage():
+    """Copy the reference's CUDA forward model, unmodified, into oracle/_ref/src/.
+    Returns the staged header's path, or None when neither the checkout nor an
+    earlier staged copy exists."""
+    ref = reference_dir()
+    if ref:
+        os.makedirs(SRC, exist_ok=True)
+        for rel in STAGED:
+            src = os.path.join(ref, rel)
+            dst = os.path.join(SRC, os.path.basename(rel))
+            if not os.path.exists(dst) or _sha(dst) != _sha(src):
+                shutil.copyfile(src, dst)
+    hdr = os.path.join(SRC, "CUDAISMLMC.h")
+    return hdr if os.path.exists(hdr) else None
+
+
+def build_praxis():
+    ref = reference_dir()
+    if not ref:
+        return None
+    src = os.path.join(ref, "CUDA", "praxis.cpp")
     if not os.path.exists(src):
         return None
     os.makedirs(OUT, exist_ok=True)
@@ -33,5 +82,37 @@ def build():
     return lib
 
 
+def build_refcuda():
+    """Compile the timing harness against the staged reference header for
+    sm_103a.  The only change to the reference's build is -DclockRate=major:
+    CUDA 13 removed cudaDeviceProp::clockRate, which the reference's
+    CUDABasicProperties() (CUDAISMLMC.h:29-39, never called by the harness)
+    prints.  Returns the binary's path, or None without a staged header."""
+    hdr = stage()
+    if not hdr:
+        return None
+    if os.path.exists(REFCUDA_BIN) and os.path.getmtime(REFCUDA_BIN) >= max(
+            os.path.getmtime(hdr), os.path.getmtime(HARNESS)):
+        return REFCUDA_BIN
+    nvcc = os.environ.get("NVCC") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        nvcc = "nvcc"
+    cmd = [nvcc, "-O3", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a",
+           "-DclockRate=major", "-w", "-I" + SRC, HARNESS, "-o", REFCUDA_BIN]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference CUDA harness build failed:\n" + " ".join(cmd) + "\n" +
+                           r.stdout + r.stderr)
+    return REFCUDA_BIN
+
+
+def build():
+    """What build() of the project does with the reference: the in-place PRAXIS
+    library and the staged CUDA header (no CUDA compilation here)."""
+    stage()
+    return build_praxis()
+
+
 if __name__ == "__main__":
     print(build())
+    print(stage())

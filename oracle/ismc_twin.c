@@ -412,6 +412,7 @@ static void* work_fn(void* arg) {
  * so the result does not depend on the thread count. */
 int twin_run(const ismc_instance* inst, uint32_t max_events, int threads, ismc_tally* out) {
     if (!inst || !out || inst->stack.L < 1 || inst->stack.L > ISMC_MAXL) return -1;
+    if (inst->n_packets > ISMC_MAX_PACKETS) return -1;
     TwinInst I;
     prepare(inst, &I);
     if (threads < 1) threads = 1;

@@ -58,31 +58,34 @@ GLASS15 = layer(1.5, 0.0, 0.0, 0.0, 0.1)
 GLASS152 = layer(1.52, 0.0, 0.0, 0.0, 0.1)
 SLAB0 = layer(1.4, 1.0, 100.0, 0.9, 0.1)
 
-# name -> (driver, layers, spheres, N, K, base_seed)
+# name -> (driver, layers, spheres, N, K, base_seed).  64 batches per case, so
+# that the batch-mean standard error is itself known to ~9 % and the 3-sigma
+# comparison of tests/test_gpu_parity.py holds for a correct implementation
+# with the normal tail probability (0.27 % per tally).
 #   driver "ISMLMC": ISMLMC.ISMLMC (multilayer, roulette threshold 1e-4)
 #   driver "ISMC":   ISMC.ISMC     (single slab, roulette threshold 1e-3)
 CASES = {
     # benchmark workload 0: slab between two n=1.5 slides, both spheres, crosstalk
-    "bench0_slides": ("ISMLMC", [GLASS15, SLAB0, GLASS15], spheres(), 100000, 16, 1000),
+    "bench0_slides": ("ISMLMC", [GLASS15, SLAB0, GLASS15], spheres(), 400000, 64, 1000),
     # benchmark workload 1: three tissue layers between n=1.52 slides
     "bench1_multilayer": ("ISMLMC", [GLASS152,
                                      layer(1.37, 0.5, 200.0, 0.8, 0.01),
                                      layer(1.40, 2.0, 120.0, 0.9, 0.15),
                                      layer(1.44, 0.2, 50.0, 0.75, 0.3),
-                                     GLASS152], spheres(), 1000000, 32, 2000),
+                                     GLASS152], spheres(), 4000000, 64, 2000),
     # workload 0 without slides, single-slab driver, every sphere combination
-    "slab_both": ("ISMC", [SLAB0], spheres(), 100000, 16, 3000),
-    "slab_R_only": ("ISMC", [SLAB0], spheres(T=False), 100000, 16, 3100),
-    "slab_T_only": ("ISMC", [SLAB0], spheres(R=False), 100000, 16, 3200),
-    "slab_no_spheres": ("ISMC", [SLAB0], spheres(R=False, T=False), 100000, 16, 3300),
-    "slab_specular_included": ("ISMC", [SLAB0], spheres(specular_included=True), 100000, 16, 3400),
+    "slab_both": ("ISMC", [SLAB0], spheres(), 400000, 64, 3000),
+    "slab_R_only": ("ISMC", [SLAB0], spheres(T=False), 400000, 64, 3100),
+    "slab_T_only": ("ISMC", [SLAB0], spheres(R=False), 400000, 64, 3200),
+    "slab_no_spheres": ("ISMC", [SLAB0], spheres(R=False, T=False), 400000, 64, 3300),
+    "slab_specular_included": ("ISMC", [SLAB0], spheres(specular_included=True), 400000, 64, 3400),
     # the single-slab example of ISMC.py:19-50 (R sphere only)
     "ismc_example": ("ISMC", [layer(1.4, 1.78, 31.2 / 0.5, 0.5, 0.135)],
                      dict(R=True, R_pw=0.99, R_fs=0.02351, R_fp=0.054638, R_fd=0.02351,
                           R_f=0.02351 + 0.054638 + 0.02351, R_angle=math.pi / 10,
                           specular_included=False, T=False, T_pw=0.99, T_fs=0.054638,
                           T_fp=0.02351, T_fd=0.02351, T_f=0.054638 + 0.02351 + 0.02351,
-                          T_angle=0.22 * math.pi / 180), 100000, 16, 3500),
+                          T_angle=0.22 * math.pi / 180), 400000, 64, 3500),
     # the three-layer example of ISMLMC.py:20-55 (isotropic middle layer, no spheres)
     "ismlmc_example": ("ISMLMC", [layer(1.37, 1.0, 10.0 / 0.1, 0.9, 0.1),
                                   layer(1.37, 1.0, 10.0, 0.0, 0.1),
@@ -90,12 +93,12 @@ CASES = {
                        dict(R=False, R_pw=0.85, R_fs=0.1, R_fp=0.05, R_fd=0.05, R_f=0.2,
                             R_angle=math.pi / 10, specular_included=False,
                             T=False, T_pw=0.85, T_fs=0.1, T_fp=0.05, T_fd=0.05, T_f=0.2,
-                            T_angle=math.pi / 10), 100000, 16, 3600),
+                            T_angle=math.pi / 10), 400000, 64, 3600),
     # lookup-grid corners (single slab between n=1.5 slides, n=1.4, g=0.9)
     "grid_low_albedo_thin": ("ISMLMC", [GLASS15, layer(1.4, 10.0, 1.0 / 0.1, 0.9, 0.05), GLASS15],
-                             spheres(), 100000, 16, 3700),
+                             spheres(), 400000, 64, 3700),
     "grid_high_albedo_thick": ("ISMLMC", [GLASS15, layer(1.4, 0.01, 100.0 / 0.1, 0.9, 0.2), GLASS15],
-                               spheres(), 20000, 16, 3800),
+                               spheres(), 80000, 64, 3800),
     # five tissue layers with distinct indices, slides n=1.5, mixed anisotropy
     "five_layer_mixed": ("ISMLMC", [GLASS15,
                                     layer(1.33, 0.3, 80.0, 0.8, 0.05),
@@ -103,10 +106,10 @@ CASES = {
                                     layer(1.38, 0.05, 150.0, 0.95, 0.1),
                                     layer(1.50, 1.0, 20.0, 0.0, 0.03),
                                     layer(1.36, 0.5, 60.0, 0.9, 0.12),
-                                    GLASS15], spheres(), 50000, 16, 3900),
+                                    GLASS15], spheres(), 200000, 64, 3900),
     # tissue directly against ambient on both faces, both spheres, thicker slab
     "bare_two_layer": ("ISMLMC", [layer(1.4, 0.5, 50.0, 0.85, 0.1),
-                                  layer(1.33, 0.2, 30.0, 0.7, 0.2)], spheres(), 100000, 16, 4000),
+                                  layer(1.33, 0.2, 30.0, 0.7, 0.2)], spheres(), 400000, 64, 4000),
 }
 
 

@@ -24,6 +24,42 @@ def test_header_and_bindings_agree():
     assert declared == set(_abi.EXPORTS), declared ^ set(_abi.EXPORTS)
 
 
+def test_header_constants_match_bindings():
+    hdr = open(os.path.join(ROOT, "include", "ismc.h")).read()
+
+    def define(name):
+        m = re.search(r"^#define\s+" + name + r"\s+(\S+)", hdr, re.M)
+        assert m, name
+        return int(m.group(1).rstrip("uUlL").strip("()"), 0)
+    assert define("ISMC_NOALLOC_MAX_INST") == _abi.NOALLOC_MAX_INST
+    assert define("ISMC_MAX_PACKETS") == _abi.MAX_PACKETS
+    assert define("ISMC_MAXL") == _abi.MAXL
+    assert define("ISMC_ABI_VERSION") == _abi.ABI_VERSION
+    for code, name in _abi.ERR_NAMES.items():
+        if code:
+            assert define("ISMC_ERR_" + name) == code, name
+
+
+def test_validate_refuses_without_a_launch(lib):
+    """Host-side checks need no GPU: an instance claiming more packets than
+    64-bit tallies can hold (5e9 > 2^31) is refused with ISMC_ERR_CAPACITY,
+    the limit itself is accepted, and a bad roulette is an invalid argument."""
+    from ismc_gb300 import Layer, Spheres, make_instance
+    good = make_instance([Layer(1.4, 1.0, 100.0, 0.9, 0.1)], Spheres(), _abi.MAX_PACKETS, seed=1)
+    big = make_instance([Layer(1.4, 1.0, 100.0, 0.9, 0.1)], Spheres(), 5_000_000_000, seed=1)
+    roul = make_instance([Layer(1.4, 1.0, 100.0, 0.9, 0.1)], Spheres(), 10, seed=1,
+                         roulette_threshold=0.5, roulette_m=10.0)
+    arr = (_abi.Instance * 3)(good, big, roul)
+    st = (C.c_int32 * 3)()
+    rc = lib.ismc_validate(arr, 3, st)
+    assert rc == _abi.ERR_CAPACITY
+    assert list(st) == [_abi.OK, _abi.ERR_CAPACITY, _abi.ERR_INVALID_ARG]
+    buf = C.create_string_buffer(512)
+    lib.ismc_last_error(None, buf, 512)
+    assert b"5000000000 packets exceed" in buf.value
+    assert lib.ismc_validate(arr, 1, None) == _abi.OK
+
+
 def test_exports_and_layout(lib):
     for name in _abi.EXPORTS:
         assert hasattr(lib, name), name

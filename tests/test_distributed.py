@@ -34,8 +34,13 @@ def _worker(rank, world, port, n, q):
                  cases.case_instance(G["five_layer_mixed"], n // 3, seed=6, stream=2)]
         mine = [oracle.twin_run(D.shard_instance(x, rank, world), threads=2) for x in insts]
         merged = D.allreduce_tallies(mine)
+        # the check bench.py runs under torchrun, with the twin as the engine
+        _, same = D.sharded_run_check(lambda x: oracle.twin_run(x, threads=2),
+                                      cases.case_instance(G["bench1_multilayer"], n // 4, seed=7),
+                                      rank, world)
         if rank == 0:
-            q.put([(list(m.sum), list(m.sumsq), m.steps, m.events, m.n, m.status) for m in merged])
+            q.put(([(list(m.sum), list(m.sumsq), m.steps, m.events, m.n, m.status) for m in merged],
+                   same))
     finally:
         dist.destroy_process_group()
 
@@ -50,7 +55,7 @@ def test_two_rank_merge_equals_single_process():
     procs = [ctx.Process(target=_worker, args=(r, 2, port, n, q)) for r in range(2)]
     for p in procs:
         p.start()
-    got = q.get(timeout=300)
+    got, same = q.get(timeout=300)
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
@@ -60,6 +65,7 @@ def test_two_rank_merge_equals_single_process():
     for (s, q2, st, ev, nn, status), w in zip(got, whole):
         assert s == list(w.sum) and q2 == list(w.sumsq)
         assert st == w.steps and ev == w.events and nn == w.n and status == w.status
+    assert same is True
 
 
 def test_shard_range_covers_exactly():

@@ -82,11 +82,14 @@ def test_run_driver_uses_dropin_and_stand_ins(tmp_path, monkeypatch):
         assert (tmp_path / "t.npz").exists()
 
 
-REF = "/root/reference"
+def _reference_dir():
+    from oracle import build_ref
+    return build_ref.reference_dir()
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference drivers not present")
+@pytest.mark.skipif(_reference_dir() is None, reason="reference drivers not present")
 def test_reference_drivers_patch_and_compile():
+    REF = _reference_dir()
     for name, sub in (("lookup.py", "Lookup"), ("minimization.py", "Minimization")):
         p = os.path.join(REF, sub, name)
         with open(p) as f:

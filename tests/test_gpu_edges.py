@@ -78,3 +78,28 @@ def test_batch_size_limits(engine):
     assert all(t.n == 1 and t.status == 0 for t in res)
     for k in (0, 1, 2499, 4999):
         assert _same(res[k], oracle.twin_run(insts[k]))
+
+
+def test_packet_count_beyond_tally_headroom(engine):
+    """An instance of more than ISMC_MAX_PACKETS (2^31) packets could wrap its
+    64-bit sums.  The host-pointer entry point refuses the batch before any
+    launch; the device-pointer entry point runs the rest of the batch and marks
+    that instance ISMC_ERR_CAPACITY with n = 0."""
+    import torch
+    from ismc_gb300 import IsmcError
+    good = make_instance([Layer(1.4, 1.0, 100.0, 0.9, 0.1)], bench_spheres(), 30_000, seed=8)
+    big = make_instance([Layer(1.4, 1.0, 100.0, 0.9, 0.1)], bench_spheres(), 5_000_000_000, seed=8)
+    with pytest.raises(IsmcError) as e:
+        engine.run_batch_raw([good, big])
+    assert e.value.code == _abi.ERR_CAPACITY
+    arr = (_abi.Instance * 2)(good, big)
+    d_in = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).cuda()
+    d_out = torch.zeros(2 * C.sizeof(_abi.Tally), dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    engine.run_batch_device(d_in.data_ptr(), 2, d_out.data_ptr(), s.cuda_stream)
+    s.synchronize()
+    out = (_abi.Tally * 2).from_buffer_copy(d_out.cpu().numpy().tobytes())
+    assert _same(out[0], oracle.twin_run(good)) and out[0].status == 0
+    assert out[1].status == _abi.ERR_CAPACITY and out[1].n == 0 and list(out[1].sum) == [0] * 5
+    # the context stays usable
+    assert engine.run_batch_raw([good])[0].status == 0

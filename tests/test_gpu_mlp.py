@@ -124,3 +124,25 @@ def test_mlp_training_lowers_loss():
         assert np.sqrt(np.mean((pred - Y[:4096]) ** 2)) < 0.02
     finally:
         s.close()
+
+
+def test_pipeline_wait_limit_runs_out_and_context_recovers(sur):
+    """With the wait limit at 0 every product's first pipeline wait gives up at
+    once: the forward pass returns ISMC_ERR_INTERNAL (after each block let its
+    requested tiles land and freed its TMEM).  With the limit restored, the
+    same context computes the same outputs as before."""
+    from ismc_gb300 import IsmcError, _abi
+    from oracle import mlp64
+    rng = np.random.default_rng(5)
+    x = (mlp64.LO + (mlp64.HI - mlp64.LO) * rng.random((256, 5))).astype(np.float32)
+    before = sur.forward(x).cpu().numpy()
+    assert sur.lib.ismc_mlp_set_wait_limit(sur.h, 0) == 0
+    try:
+        with pytest.raises(IsmcError) as e:
+            sur.forward(x)
+        assert e.value.code == _abi.ERR_INTERNAL
+        assert "timed out" in str(e.value)
+    finally:
+        assert sur.lib.ismc_mlp_set_wait_limit(sur.h, 1 << 22) == 0
+    after = sur.forward(x).cpu().numpy()
+    assert np.array_equal(before, after)

@@ -72,6 +72,38 @@ def test_noalloc_matches_device_entry_twice():
     assert [_key(t) for t in _tallies(out1, n)] == want
 
 
+def test_noalloc_full_capacity_batch():
+    """Exactly ISMC_NOALLOC_MAX_INST instances: every slot of the fixed array
+    (and the last prefix word) is used, and the prefix scan gives each of its
+    threads one instance.  Small uneven instances tile the golden cases."""
+    import numpy as np
+    import torch
+    from ismc_gb300 import Engine
+    lib = load_library()
+    G = cases.golden()
+    names = sorted(G)
+    rng = np.random.default_rng(11)
+    n = _abi.NOALLOC_MAX_INST
+    insts = [cases.case_instance(G[names[k % len(names)]], int(rng.integers(0, 400)), seed=31,
+                                 stream=k, mode="physical" if k % 5 == 0 else "compat")
+             for k in range(n)]
+    raw = bytes((_abi.Instance * n)(*insts))
+    d_in = torch.frombuffer(bytearray(raw), dtype=torch.uint8).cuda()
+    size = n * C.sizeof(_abi.Tally)
+    ref = torch.zeros(size, dtype=torch.uint8, device="cuda")
+    out = torch.full((size,), 0x5A, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    with Engine(0) as eng:
+        eng.run_batch_device(d_in.data_ptr(), n, ref.data_ptr(), stream.cuda_stream)
+    rc = lib.ismc_run_batch_noalloc(C.c_void_p(d_in.data_ptr()), n, None,
+                                    C.c_void_p(out.data_ptr()), C.c_void_p(stream.cuda_stream))
+    assert rc == 0
+    stream.synchronize()
+    want = [_key(t) for t in _tallies(ref, n)]
+    assert [_key(t) for t in _tallies(out, n)] == want
+    assert sum(t[7] for t in want) == sum(int(x.n_packets) for x in insts)
+
+
 def test_noalloc_rejects_batches_beyond_capacity():
     lib = load_library()
     rc = lib.ismc_run_batch_noalloc(C.c_void_p(16), _abi.NOALLOC_MAX_INST + 1, None, C.c_void_p(16),
