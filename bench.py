@@ -645,11 +645,22 @@ def run_other_workload(args):
                 "1-5 layer stacks, budgets log-uniform 1e5-1e7 x scale, one persistent launch",
                 "scale": s}, "result": r}
     else:
-        sur, r = benchmarks.run_surrogate(
-            eng, n_samples=int((1 << 20) * s) // 4096 * 4096 or 4096,
-            packets=max(1000, int(100_000 * min(1.0, s * 4))), epochs=args.epochs,
-            heldout=32 if s >= 1 else 12,
-            heldout_packets=10_000_000 if s >= 1 else 1_000_000)
+        if args.load_surrogate:
+            # a network trained and saved by an earlier run of this workload
+            import numpy as np
+            from ismc_gb300.surrogate import Surrogate
+            sur = Surrogate(0, max_batch=4096, seed=42)
+            sur.set_params(np.load(args.load_surrogate))
+            r = {"loaded": args.load_surrogate}
+        else:
+            sur, r = benchmarks.run_surrogate(
+                eng, n_samples=int((1 << 20) * s) // 4096 * 4096 or 4096,
+                packets=max(1000, int(100_000 * min(1.0, s * 4))), epochs=args.epochs,
+                heldout=32 if s >= 1 else 12,
+                heldout_packets=10_000_000 if s >= 1 else 1_000_000)
+        if args.save_surrogate:
+            import numpy as np
+            np.save(args.save_surrogate, sur.get_params())
         line = {"workload": "surrogate", "config": {"scale": s, "epochs": args.epochs},
                 "result": r}
         if args.workload == "solve":
@@ -681,6 +692,10 @@ def main():
                     default="forward")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="size factor for the secondary workloads (1 = full benchmark size)")
+    ap.add_argument("--save-surrogate", default=None,
+                    help="save the trained surrogate's parameters (.npy) here")
+    ap.add_argument("--load-surrogate", default=None,
+                    help="use saved surrogate parameters (.npy) instead of training")
     ap.add_argument("--epochs", type=int, default=20,
                     help="training epochs of the surrogate (surrogate and solve workloads)")
     args = ap.parse_args()

@@ -120,70 +120,101 @@ def run_surrogate(engine, n_samples=1 << 20, packets=100_000, epochs=20, batch=4
 
 
 def run_solve(engine, sur, n_meas=10000, n_plain=200, seed=4, verify_packets=1_000_000,
-              plain_packets=100_000):
-    """Plain path on a subsample and surrogate-assisted path on all measurements."""
+              plain_packets=100_000, conv_packets=1_000_000, n_conv_repeat=100,
+              anchor_packets=500_000):
+    """Inverse solves of the benchmark's synthetic measurements, four ways.
+
+    plain       PRAXIS on the reference's cost with `plain_packets` per
+                objective (the benchmark's plain path), on the first n_plain
+                measurements: the speed baseline.
+    converged   the same minimisation with `conv_packets` per objective (common
+                random numbers) and a 5x tighter tolerance, started from the
+                plain answers: the accuracy yardstick, a plain-path answer with
+                the objective's Monte Carlo noise made small.  It is run again
+                with independent streams on the first n_conv_repeat solves:
+                the two runs' difference is the agreement any Monte Carlo
+                estimator of that minimum can reach.
+    surrogate   the surrogate path minimising the plain path's cost, every solve
+                anchored to Monte Carlo (`anchor_packets`), verified with
+                `verify_packets`, on all measurements: the headline.
+    chi2        the surrogate path minimising chi^2 (residuals in units of the
+                measurement noise) with the goodness-of-fit test, no anchoring."""
     from .surrogate import sample_stack, surrogate_solve
     truth, meas = make_measurements(engine, n_meas, seed=seed)
     sig = np.array([0.002, 0.002, 0.0005])
     sph = bench_spheres()
+    stack = sample_stack(1.0, 10.0, 0.9, 0.1, 1.4)
+
+    def mmeas(i):
+        return (meas[i, 0], None, meas[i, 1], meas[i, 2])
+
     # plain path: PRAXIS + 1e5-packet MC objective, batched across solves
     k = min(n_plain, n_meas)
-    reqs = [make_solve(sample_stack(1.0, 10.0, 0.9, 0.1, 1.4), 1, sph, plain_packets,
-                       (meas[i, 0], None, meas[i, 1], meas[i, 2]), x0=(0.3, 10.0), seed=seed + i,
+    reqs = [make_solve(stack, 1, sph, plain_packets, mmeas(i), x0=(0.3, 10.0), seed=seed + i,
                        lo=SOLVE_LO, hi=SOLVE_HI, max_evals=400) for i in range(k)]
     t0 = time.perf_counter()
     outp = engine.solve_batch(reqs)
     t_plain = time.perf_counter() - t0
     xp = np.array([[o.x[0], o.x[1]] for o in outp])
     ev = np.array([o.evals for o in outp])
+
+    # converged plain path (yardstick), and its repeat with independent streams
+    def converged(idx, seed0, x0s):
+        rq = [make_solve(stack, 1, sph, conv_packets, mmeas(i), x0=tuple(x0s[j]), seed=seed0 + i,
+                         lo=SOLVE_LO, hi=SOLVE_HI, max_evals=600, h0=0.2, t0=2e-4)
+              for j, i in enumerate(idx)]
+        out = engine.solve_batch(rq)
+        return np.array([[o.x[0], o.x[1]] for o in out]), np.array([o.evals for o in out])
+
+    t0 = time.perf_counter()
+    xc, evc = converged(range(k), seed + 20000, xp)
+    t_conv = time.perf_counter() - t0
+    kr = min(n_conv_repeat, k)
+    xc2, _ = converged(range(kr), seed + 40000, xp[:kr])
+
     # surrogate path on every measurement (after a short warm-up of its kernels)
-    surrogate_solve(sur, engine, meas[:64], sig, verify_packets=1000, fallback=False, seed=seed)
+    surrogate_solve(sur, engine, meas[:64], sig, verify_packets=1000, anchor_packets=1000,
+                    fallback=False, seed=seed, objective="reference")
     t1 = time.perf_counter()
     rs = surrogate_solve(sur, engine, meas, sig, verify_packets=verify_packets,
-                         plain_packets=plain_packets, seed=seed + 99)
+                         plain_packets=plain_packets, seed=seed + 99, objective="reference",
+                         anchor_packets=anchor_packets)
     t_sur = time.perf_counter() - t1
     xs = rs["x"]
-    # the same surrogate path minimising the plain path's cost instead of chi^2
-    rc = surrogate_solve(sur, engine, meas, sig, verify_packets=verify_packets,
-                         plain_packets=plain_packets, seed=seed + 99, objective="reference")
+    # the chi^2 variant without anchoring (goodness-of-fit test)
+    t2 = time.perf_counter()
+    r2 = surrogate_solve(sur, engine, meas, sig, verify_packets=verify_packets,
+                         plain_packets=plain_packets, seed=seed + 99, objective="chi2")
+    t_chi2 = time.perf_counter() - t2
 
     def rel(x, t):
         e = np.abs(x / t - 1)
         return {"median": np.median(e, 0).tolist(), "p90": np.percentile(e, 90, 0).tolist(),
                 "within_2pct": np.mean(e <= 0.02, 0).tolist()}
 
-    # noise-free measurements: the two paths then differ only by the plain
-    # objective's Monte Carlo noise and the surrogate's error
-    m0 = min(n_meas, 1000)
-    k0 = min(k, 200)
-    truth0, meas0 = make_measurements(engine, m0, seed=seed + 17, noise=(0.0, 0.0, 0.0))
-    reqs0 = [make_solve(sample_stack(1.0, 10.0, 0.9, 0.1, 1.4), 1, sph, plain_packets,
-                        (meas0[i, 0], None, meas0[i, 1], meas0[i, 2]), x0=(0.3, 10.0),
-                        seed=seed + 5000 + i, lo=SOLVE_LO, hi=SOLVE_HI, max_evals=400)
-             for i in range(k0)]
-    xp0 = np.array([[o.x[0], o.x[1]] for o in engine.solve_batch(reqs0)])
-    r0 = surrogate_solve(sur, engine, meas0, sig, verify_packets=verify_packets,
-                         plain_packets=plain_packets, seed=seed + 199)
-    noise_free = {"measurements": m0, "plain_subsample": k0,
-                  "plain_rel_err_vs_truth": rel(xp0, truth0[:k0]),
-                  "surrogate_rel_err_vs_truth": rel(r0["x"], truth0),
-                  "surrogate_vs_plain_rel_diff": rel(r0["x"][:k0], xp0),
-                  "fallback_rate": float(r0["fallback"].mean())}
-
-    return {"measurements": n_meas, "plain_subsample": k, "objective": "chi2",
-            "noise_free": noise_free,
+    return {"measurements": n_meas, "plain_subsample": k, "converged_repeat": kr,
+            "packets": {"plain": plain_packets, "converged": conv_packets,
+                        "anchor": anchor_packets, "verify": verify_packets},
             "plain_solves_per_s": k / t_plain, "plain_evals_mean": float(ev.mean()),
-            "plain_rel_err_vs_truth": rel(xp, truth[:k]),
+            "converged_solves_per_s": k / t_conv, "converged_evals_mean": float(evc.mean()),
             "surrogate_solves_per_s": n_meas / t_sur,
-            "surrogate_rel_err_vs_truth": rel(xs, truth),
+            "speedup": (n_meas / t_sur) / (k / t_plain),
+            # the headline: the surrogate path against the converged plain path
+            "surrogate_vs_converged_rel_diff": rel(xs[:k], xc),
+            "converged_self_spread_rel_diff": rel(xc2, xc[:kr]),
+            "plain_vs_converged_rel_diff": rel(xp, xc),
             "surrogate_vs_plain_rel_diff": rel(xs[:k], xp),
-            "reference_objective": {"rel_err_vs_truth": rel(rc["x"], truth),
-                                    "vs_plain_rel_diff": rel(rc["x"][:k], xp),
-                                    "fallback_rate": float(rc["fallback"].mean()),
-                                    "solves_per_s": n_meas / rc["timing"]["total_s"]},
+            "surrogate_rel_err_vs_truth": rel(xs, truth),
+            "converged_rel_err_vs_truth": rel(xc, truth[:k]),
+            "plain_rel_err_vs_truth": rel(xp, truth[:k]),
             "corrected_rate": float(rs["corrected"].mean()),
             "fallback_rate": float(rs["fallback"].mean()), "surrogate_timing": rs["timing"],
-            "speedup": (n_meas / t_sur) / (k / t_plain)}
+            "surrogate_mc_packets_per_solve": rs["mc_packets"] / n_meas,
+            "chi2": {"solves_per_s": n_meas / t_chi2,
+                     "rel_err_vs_truth": rel(r2["x"], truth),
+                     "vs_converged_rel_diff": rel(r2["x"][:k], xc),
+                     "corrected_rate": float(r2["corrected"].mean()),
+                     "fallback_rate": float(r2["fallback"].mean())}}
 
 
 # Algorithmic multiply-adds per training row of the 5 -> 256 -> 256 -> 256 -> 6

@@ -128,7 +128,7 @@ def gpu_makelookup(R_d, T_d, R_d_std, T_d_std, N, uncertainty=True, M=100, metho
     return mua_t, ua, mus_t, us, Rv, Tv, pts, pts.copy()
 
 
-def run_driver(path, argv, keep_quirks=False, gpu_tables=False):
+def run_driver(path, argv, keep_quirks=False, gpu_tables=False, numpy_seed=None, ismc_seed=None):
     path = os.path.abspath(path)
     name = os.path.basename(path)
     if name not in ("lookup.py", "minimization.py"):
@@ -144,6 +144,15 @@ def run_driver(path, argv, keep_quirks=False, gpu_tables=False):
     if gpu_tables:
         gpu_makelookup.driver_globals = g
         g["makelookup"] = gpu_makelookup
+    # reproducible runs: the drivers draw their input distributions from
+    # numpy's global generator, and the drop-in ISMC's k-th call uses Philox
+    # stream k of its seed
+    if numpy_seed is not None:
+        import numpy as np
+        np.random.seed(int(numpy_seed))
+    if ismc_seed is not None:
+        from ismc_gb300.dropin import _common
+        _common.seed(int(ismc_seed))
     with warnings.catch_warnings():          # the drivers' "\m" in plot labels
         warnings.simplefilter("ignore", SyntaxWarning)
         code = compile(src, path, "exec")
@@ -158,8 +167,12 @@ def main(argv=None):
                     help="do not fix the two driver bugs (T_u_exact_unc, mu_s' axis base)")
     ap.add_argument("--gpu-tables", action="store_true",
                     help="lookup.py: build the tables with the GPU make_lookup")
+    ap.add_argument("--numpy-seed", type=int, default=None,
+                    help="seed numpy's global generator before the driver runs")
+    ap.add_argument("--ismc-seed", type=int, default=None,
+                    help="seed of the drop-in ISMC's call sequence")
     a, rest = ap.parse_known_args(argv)
-    run_driver(a.driver, rest, a.keep_quirks, a.gpu_tables)
+    run_driver(a.driver, rest, a.keep_quirks, a.gpu_tables, a.numpy_seed, a.ismc_seed)
 
 
 if __name__ == "__main__":

@@ -246,24 +246,43 @@ def objective_weights(meas, sigma, objective="chi2"):
 
 def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=10, verify_packets=1_000_000,
                     seed=7, fallback=True, correct=True, plain_packets=100_000, plain_max_evals=400,
-                    objective="chi2"):
+                    objective="chi2", anchor_packets=0, anchor_steps=5, test=None):
     """Solve many measurements [m x 3] of (R_d, T_d, T_u) with noise sigma (3,).
 
     (1) The surrogate on a 48 x 48 (ln mu_a, ln mu_s') grid proposes a start;
-    (2) Gauss-Newton steps on the surrogate refine it; (3) one Monte Carlo run
-    of `verify_packets` checks it.  (3b) With `correct`, a solve that misses
-    by more than 3 sigma takes the Monte Carlo-minus-surrogate difference at
-    its point as an output offset, re-solves on the offset surrogate and is
-    verified again.  (4) What still misses falls back to the plain path
-    (PRAXIS on Monte Carlo).  Steps (1)-(3b) minimise `objective` (see
-    objective_weights); the 3-sigma test of the verification uses sigma.  Returns dict with x [m x 2] (mu_a, mu_s'), the
-    verified MC values, masks of corrected and fallback solves, and timings."""
+    (2) Gauss-Newton steps on the surrogate refine it.  (2b) With
+    `anchor_packets`, every solve is anchored to Monte Carlo: one run of that
+    many packets at its point gives the Monte Carlo-minus-surrogate difference
+    there, and `anchor_steps` more Gauss-Newton steps minimise on the surrogate
+    shifted by it -- the local bias of the network is then gone, and the answer
+    approaches the minimum of the Monte Carlo objective itself.  (3) One Monte
+    Carlo run of `verify_packets` verifies the final point.  (3b) With
+    `correct`, a solve that fails the test is re-anchored at its point by that
+    verification, re-solved and verified again.  (4) What still fails falls
+    back to the plain path (PRAXIS on Monte Carlo), started from the
+    surrogate's answer.
+
+    Steps (1)-(3b) minimise `objective` (see objective_weights).  The test of
+    step (3) is `test`: "fit" (the default for chi2) asks every verified value
+    to lie within 3 sigma of the measurement, sqrt(sigma^2 + se^2); "surrogate"
+    (the default otherwise) asks the surrogate's prediction at the final point,
+    anchor offset included, to lie within 3 standard errors of the verifying
+    Monte Carlo run.  Returns dict with x [m x 2] (mu_a, mu_s'), the verified
+    MC values, masks of corrected and fallback solves, and timings."""
     import torch
     meas = np.asarray(meas, dtype=np.float64)
     sig = np.asarray(sigma, dtype=np.float64)
     wts = objective_weights(meas, sig, objective)
+    test = test or ("fit" if objective == "chi2" else "surrogate")
+    if test not in ("fit", "surrogate"):
+        raise ValueError(f"unknown test {test!r}")
     m = len(meas)
     T = {}
+
+    def predict(x):
+        Xi = np.concatenate([x, np.tile([g, d, n], (len(x), 1))], 1)
+        return sur.forward(Xi).cpu().numpy()[:, :3].astype(np.float64)
+
     t0 = time.perf_counter()
     # (1) grid proposal, shared surrogate evaluations for all measurements
     grid = _grid()
@@ -281,28 +300,41 @@ def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=10, 
     t1 = time.perf_counter()
     x = _gauss_newton(sur, x, meas, wts, 0.0, gn_steps, g, d, n)
     T["gauss_newton_s"] = time.perf_counter() - t1
+    # (2b) anchor every solve to Monte Carlo at its point
+    t1 = time.perf_counter()
+    off = np.zeros_like(meas)
+    off_se = np.zeros_like(meas)
+    if anchor_packets:
+        Va, off_se = _verify(engine, x, g, d, n, anchor_packets, seed + 3, stream0=2 * m)
+        off = Va - predict(x)
+        x = _gauss_newton(sur, x, meas, wts, off, anchor_steps, g, d, n)
+    T["anchor_s"] = time.perf_counter() - t1
     # (3) Monte Carlo verification at the answers: one batched launch
     t2 = time.perf_counter()
     V, VS = _verify(engine, x, g, d, n, verify_packets, seed)
+    pred = predict(x) + off
     T["verify_s"] = time.perf_counter() - t2
 
-    def missed(V, VS):
-        return np.any(np.abs(V - meas) > 3 * np.sqrt(sig ** 2 + VS ** 2), axis=1)
+    def failed(V, VS, pred, pred_se):
+        if test == "fit":
+            return np.any(np.abs(V - meas) > 3 * np.sqrt(sig ** 2 + VS ** 2), axis=1)
+        return np.any(np.abs(V - pred) > 3 * np.sqrt(VS ** 2 + pred_se ** 2), axis=1)
 
-    miss = missed(V, VS)
+    miss = failed(V, VS, pred, off_se)
     corrected = np.zeros(m, dtype=bool)
-    # (3b) offset correction of the misses, verified again
+    # (3b) re-anchor the failures at their verified values, verify again
     t3 = time.perf_counter()
     if correct and miss.any():
         idx = np.nonzero(miss)[0]
         xi = x[idx]
-        Xi = np.concatenate([xi, np.tile([g, d, n], (len(xi), 1))], 1)
-        off = V[idx] - sur.forward(Xi).cpu().numpy()[:, :3].astype(np.float64)
-        xi = _gauss_newton(sur, xi, meas[idx], wts[idx], off, gn_steps, g, d, n)
+        oi = V[idx] - predict(xi)
+        xi = _gauss_newton(sur, xi, meas[idx], wts[idx], oi, gn_steps, g, d, n)
         Vi, VSi = _verify(engine, xi, g, d, n, verify_packets, seed + 1, stream0=m)
         x[idx], V[idx], VS[idx] = xi, Vi, VSi
+        pred[idx] = predict(xi) + oi
+        off_se[idx] = VS[idx]
         corrected[idx] = True
-        miss = missed(V, VS)
+        miss = failed(V, VS, pred, off_se)
     T["correct_s"] = time.perf_counter() - t3
     # (4) fallback to the plain path for what still misses
     t4 = time.perf_counter()
@@ -322,7 +354,9 @@ def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=10, 
         fallback_evals = 0
     T["fallback_s"] = time.perf_counter() - t4
     T["total_s"] = time.perf_counter() - t0
-    # Monte Carlo packets spent: verification, re-verification, fallback objectives
-    mc = (m + int(corrected.sum())) * verify_packets + fallback_evals * plain_packets
+    # Monte Carlo packets spent: anchors, verification, re-verification, fallback objectives
+    mc = (m * (1 if anchor_packets else 0)) * anchor_packets + \
+        (m + int(corrected.sum())) * verify_packets + fallback_evals * plain_packets
     return {"x": xr, "verified": V, "verified_se": VS, "corrected": corrected, "fallback": miss,
-            "timing": T, "mc_packets": mc, "fallback_evals": fallback_evals}
+            "timing": T, "mc_packets": mc, "fallback_evals": fallback_evals,
+            "objective": objective, "test": test, "anchor_packets": anchor_packets}

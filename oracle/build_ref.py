@@ -10,6 +10,11 @@
                                  GPU machine, where the reference checkout is
                                  absent.  It is never committed (oracle/_ref/ is
                                  git-ignored) and never edited.
+  oracle/_ref/drivers/           byte-for-byte copies of the reference's driver
+                                 scripts and their example configurations
+                                 (Lookup/lookup.py, Minimization/minimization.py,
+                                 */example.ini), staged the same way for the
+                                 end-to-end driver tests on the GPU machine
   oracle/_ref/refcuda_bench      oracle/refcuda_bench.cu, the project's timing
                                  harness, compiled against the staged header
                                  for sm_103a (build_refcuda(), on the GPU
@@ -31,6 +36,10 @@ DEFAULT_REFERENCE_DIR = "/root/reference"
 # the reference's CUDA forward model: kernel CUDAISMLMC (CUDAISMLMC.h:316-654)
 # and its host wrapper ISMLMC() (CUDAISMLMC.h:656-755)
 STAGED = ("CUDA/CUDAISMLMC.h",)
+# the reference's driver scripts (run unmodified through ismc_gb300.dropin.drivers)
+DRIVERS = ("Lookup/lookup.py", "Lookup/example.ini", "Minimization/minimization.py",
+           "Minimization/example.ini")
+DRIVERS_DIR = os.path.join(OUT, "drivers")
 HARNESS = os.path.join(HERE, "refcuda_bench.cu")
 REFCUDA_BIN = os.path.join(OUT, "refcuda_bench")
 
@@ -52,14 +61,23 @@ def stage():
     earlier staged copy exists."""
     ref = reference_dir()
     if ref:
-        os.makedirs(SRC, exist_ok=True)
-        for rel in STAGED:
+        copies = [(rel, os.path.join(SRC, os.path.basename(rel))) for rel in STAGED]
+        copies += [(rel, os.path.join(DRIVERS_DIR, rel)) for rel in DRIVERS]
+        for rel, dst in copies:
             src = os.path.join(ref, rel)
-            dst = os.path.join(SRC, os.path.basename(rel))
+            os.makedirs(os.path.dirname(dst), exist_ok=True)
             if not os.path.exists(dst) or _sha(dst) != _sha(src):
                 shutil.copyfile(src, dst)
     hdr = os.path.join(SRC, "CUDAISMLMC.h")
     return hdr if os.path.exists(hdr) else None
+
+
+def staged_driver(rel):
+    """Path of a staged reference driver file (e.g. "Minimization/minimization.py"),
+    or None where it was never staged."""
+    stage()
+    p = os.path.join(DRIVERS_DIR, rel)
+    return p if os.path.exists(p) else None
 
 
 def build_praxis():
