@@ -653,11 +653,11 @@ def run_other_workload(args):
             sur.set_params(np.load(args.load_surrogate))
             r = {"loaded": args.load_surrogate}
         else:
+            hg = args.heldout if args.heldout is not None else (32 if s >= 1 else 12)
             sur, r = benchmarks.run_surrogate(
                 eng, n_samples=int((1 << 20) * s) // 4096 * 4096 or 4096,
                 packets=max(1000, int(100_000 * min(1.0, s * 4))), epochs=args.epochs,
-                heldout=32 if s >= 1 else 12,
-                heldout_packets=10_000_000 if s >= 1 else 1_000_000)
+                heldout=hg, heldout_packets=10_000_000 if s >= 1 else 1_000_000)
         if args.save_surrogate:
             import numpy as np
             np.save(args.save_surrogate, sur.get_params())
@@ -696,6 +696,9 @@ def main():
                     help="save the trained surrogate's parameters (.npy) here")
     ap.add_argument("--load-surrogate", default=None,
                     help="use saved surrogate parameters (.npy) instead of training")
+    ap.add_argument("--heldout", type=int, default=None,
+                    help="points per axis of the surrogate's held-out grid (default 32 at full "
+                         "scale; each point is a 1e7-packet run)")
     ap.add_argument("--epochs", type=int, default=20,
                     help="training epochs of the surrogate (surrogate and solve workloads)")
     args = ap.parse_args()
