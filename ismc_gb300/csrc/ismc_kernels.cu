@@ -385,6 +385,36 @@ __device__ __forceinline__ float4 ismc_lq(const DevInst& I, int l, int k) {
     return reinterpret_cast<const float4*>(&I.ly[l])[k];
 }
 
+// Branch statistics, compiled in only with -DISMC_BRANCH_STATS (a separate
+// library built by ismc_gb300/perf.py, never the product): for each branch of
+// the event loop, how many warp executions it had and how many lanes were
+// active in them.  ismc_branch_stats[2k] counts executions of branch k,
+// [2k+1] sums their active lanes.
+#ifdef ISMC_BRANCH_STATS
+__device__ unsigned long long ismc_branch_stats[32];
+#define ISMC_BRANCH(k)                                                                   \
+    do {                                                                                 \
+        const unsigned m_ = __activemask();                                              \
+        if ((int)(threadIdx.x & 31) == __ffs(m_) - 1) {                                  \
+            atomicAdd(&ismc_branch_stats[2 * (k)], 1ull);                                \
+            atomicAdd(&ismc_branch_stats[2 * (k) + 1], (unsigned long long)__popc(m_));  \
+        }                                                                                \
+    } while (0)
+extern "C" int ismc_branch_stats_read(unsigned long long* out) {
+    return cudaMemcpyFromSymbol(out, ismc_branch_stats, sizeof(ismc_branch_stats)) == cudaSuccess
+               ? 0 : -1;
+}
+extern "C" int ismc_branch_stats_reset(void) {
+    static const unsigned long long z[32] = {0};
+    return cudaMemcpyToSymbol(ismc_branch_stats, z, sizeof z) == cudaSuccess ? 0 : -1;
+}
+#else
+#define ISMC_BRANCH(k) do { } while (0)
+#endif
+// branch numbers of ISMC_BRANCH
+enum { ISMC_BR_ITER = 0, ISMC_BR_HANDOUT, ISMC_BR_EVENT, ISMC_BR_INCIDENT, ISMC_BR_WALK,
+       ISMC_BR_INTERFACE, ISMC_BR_INTERACTION, ISMC_BR_SPIN, ISMC_BR_SPHERE, ISMC_BR_FIN };
+
 extern "C" __global__ void __launch_bounds__(ISMC_MAX_THREADS)
 ismc_propagate_kernel(const PropParams P) {
     extern __shared__ __align__(16) unsigned char ismc_smem[];
@@ -416,7 +446,9 @@ ismc_propagate_kernel(const PropParams P) {
     for (;;) {
         // ================================================= hand out packets
         unsigned need = __ballot_sync(ISMC_FULL, !alive);
+        ISMC_BRANCH(ISMC_BR_ITER);
         if (need) {     // every lane busy (the common case): nothing to hand out
+            ISMC_BRANCH(ISMC_BR_HANDOUT);
             while (need) {
                 if (c_next < c_end) {
                     const unsigned long long avail = c_end - c_next;
@@ -500,6 +532,7 @@ ismc_propagate_kernel(const PropParams P) {
         }
 
         // ================================================= one event
+        ISMC_BRANCH(ISMC_BR_EVENT);
         const DevInst& I = ws->slot[slot];
         const uint32_t L = I.L;
         const bool compat = I.mode == ISMC_MODE_COMPAT;
@@ -515,6 +548,7 @@ ismc_propagate_kernel(const PropParams P) {
         if (ev > P.max_events) {
             fin = 2;
         } else if (phase == PH_INCIDENT) {
+            ISMC_BRANCH(ISMC_BR_INCIDENT);
             // -------- incidence on the sample (ISMLMC.py:126-229)
             const bool top = uz > 0.0f;
             const int l = top ? 0 : (int)L - 1;
@@ -546,34 +580,76 @@ ismc_propagate_kernel(const PropParams P) {
             }
         } else {
             // -------- walk inside layer l (MLMC.py:95-200)
+            // A lane either reaches the next interface (reflect, refract or
+            // leave) or interacts inside the layer (hop, drop, roulette,
+            // spin).  In a warp both kinds nearly always occur together, so
+            // the two share one instruction stream: one division (the path to
+            // the boundary, or the Henyey-Greenstein quotient) and one square
+            // root (the refracted cosine, or sin(theta) / sin(polar)) serve
+            // both, and each lane keeps only its own results.  Every value is
+            // the same correctly rounded operation on the same operands as in
+            // a lane that computes one kind alone.
+            ISMC_BRANCH(ISMC_BR_WALK);
             const int l = layer;
             const bool down = uz > 0.0f;
-            const bool glass = (I.ly[l].lflags & ISMC_LF_GLASS) != 0u;
+            const uint32_t lf = I.ly[l].lflags;
+            const bool glass = (lf & ISMC_LF_GLASS) != 0u;
             const float4 q0 = ismc_lq(I, l, 0);     // mut, inv_mut, drop, hgc
+            const float4 q1 = ismc_lq(I, l, 1);     // hgd, hge, hga, hgb
             const float4 q2 = ismc_lq(I, l, 2);     // z_top, z_bot, eta_up, eta_dn
             const float zb = down ? q2.y : q2.x;
             // distance to the boundary along z (rounding can leave z a hair outside)
             const float dist = fmaxf(down ? zb - z : z - zb, 0.0f);
             const float auz = fabsf(uz);
             const float mut = q0.x;
-            if (glass && auz == 0.0f) {
-                fin = 2;                                   // cannot leave a slide: give up on it
-            } else if (glass || (auz > 0.0f && dist * mut <= tau * auz)) {
-                // ---- reach the interface (free path tau/mut >= dist/|uz|, no division)
+            // a slide the packet cannot leave: give up on it
+            const bool stuck = glass && auz == 0.0f;
+            // free path tau/mut >= dist/|uz|, tested without a division
+            const bool cross = !stuck && (glass || (auz > 0.0f && dist * mut <= tau * auz));
+            const float u1 = ismc_u01(r.y), u2 = ismc_u01(r.z);
+            // the one division: dist / |uz| at an interface, the HG quotient
+            // (1 - g^2) / (1 - g + 2 g u1) in an interaction
+            const float quo = __fdiv_rn(cross ? dist : q0.w, cross ? auz : __fmaf_rn(q1.y, u1, q1.x));
+            // interface: refraction geometry (ismc_fresnel_reflects, split at its root)
+            const float eta = down ? q2.w : q2.z;
+            const float s2t = (eta * eta) * (1.0f - auz * auz);
+            const bool tir = s2t >= 1.0f;
+            // interaction: polar cosine, isotropic or Henyey-Greenstein (MLMC.py:183-186)
+            float cth = (lf & ISMC_LF_ISO) ? 2.0f * u1 - 1.0f
+                                           : fminf(fmaxf(q1.z * __fmaf_rn(-quo, quo, q1.w), -1.0f), 1.0f);
+            const float s2 = fmaxf(__fmaf_rn(-cth, cth, 1.0f), 0.0f);   // sin^2 theta
+            const bool normal = auz > 0.99999f;                          // MLMC.py:190
+            // rho2 = sin^2 of the polar angle from the transverse components
+            // (= 1 - uz^2 for a unit vector; this form keeps the FP32 norm error
+            // from growing as 1/(1 - uz^2))
+            const float rho2 = __fmaf_rn(ux, ux, uy * uy);
+            const float kk = __fdiv_rn(s2, rho2);
+            // the one square root
+            const float sq = __fsqrt_rn(cross ? (tir ? 0.0f : 1.0f - s2t) : (normal ? s2 : kk));
+            if (stuck) {
+                fin = 2;
+            } else if (cross) {
+                // ---- reach the interface
+                ISMC_BRANCH(ISMC_BR_INTERFACE);
                 if (!glass) {
-                    const float d = __fdiv_rn(dist, auz);
-                    tau = fmaxf(__fmaf_rn(-d, mut, tau), 0.0f);
+                    tau = fmaxf(__fmaf_rn(-quo, mut, tau), 0.0f);
                 } else if (!compat && q0.z > 0.0f) {
-                    const float d = __fdiv_rn(dist, auz);
-                    const float wn = w * ismc_expneg(q0.z * d);
+                    const float wn = w * ismc_expneg(q0.z * quo);
                     absorbed = absorbed + (w - wn);
                     w = wn;
                 }
                 z = zb;
                 const int nl = down ? l + 1 : l - 1;
-                const float eta = down ? q2.w : q2.z;
-                float ct;
-                if (ismc_fresnel_reflects(eta, auz, u0, &ct)) {
+                // reflect-or-transmit draw without the Fresnel division (ismc_fresnel_reflects)
+                bool refl = tir;
+                if (!tir) {
+                    const float a = eta * auz, b = eta * sq;
+                    const float rsn = a - sq, rsd = a + sq, rpn = b - auz, rpd = b + auz;
+                    const float x = rsn * rpd, y = rpn * rsd, den = rsd * rpd;
+                    refl = u0 * (den * den) < 0.5f * __fmaf_rn(x, x, y * y);
+                }
+                const float ct = tir ? 0.0f : sq;
+                if (refl) {
                     uz = -uz;
                 } else if (nl < 0 || nl >= (int)L) {
                     side = nl < 0 ? 0u : 1u;
@@ -592,6 +668,7 @@ ismc_propagate_kernel(const PropParams P) {
                 }
             } else {
                 // ---- interaction inside the layer: hop, drop, roulette, spin
+                ISMC_BRANCH(ISMC_BR_INTERACTION);
                 const float s = tau * q0.y;
                 z = __fmaf_rn(s, uz, z);
                 const float dw = w * q0.z;
@@ -602,47 +679,35 @@ ismc_propagate_kernel(const PropParams P) {
                     if (u0 < I.roul_inv_m) w = w * I.roul_m;
                     else { w = 0.0f; fin = 1; }
                 }
-                if (!fin) {
-                    const float u1 = ismc_u01(r.y), u2 = ismc_u01(r.z);
-                    float cth;
-                    if (I.ly[l].lflags & ISMC_LF_ISO) {
-                        cth = 2.0f * u1 - 1.0f;
-                    } else {
-                        const float4 q1 = ismc_lq(I, l, 1);     // hgd, hge, hga, hgb
-                        const float t = __fdiv_rn(q0.w, __fmaf_rn(q1.y, u1, q1.x));
-                        cth = q1.z * __fmaf_rn(-t, t, q1.w);
-                        cth = fminf(fmaxf(cth, -1.0f), 1.0f);
-                    }
-                    float sp, cp;
-                    ismc_sincos_2pi(u2, &sp, &cp);
-                    const float s2 = fmaxf(__fmaf_rn(-cth, cth, 1.0f), 0.0f);   // sin^2 theta
-                    if (fabsf(uz) > 0.99999f) {             // MLMC.py:190-193
-                        const float sth = __fsqrt_rn(s2);
-                        ux = sth * cp;
-                        uy = sth * sp;
-                        uz = uz > 0.0f ? cth : -cth;
-                    } else {                                 // MLMC.py:194-198
-                        // rho2 = sin^2 of the polar angle from the transverse
-                        // components (= 1 - uz^2 for a unit vector; this form keeps
-                        // the FP32 norm error from growing as 1/(1 - uz^2)), and
-                        // k = sin(theta)/sin(polar) from one division and one root:
-                        //   new = k (ux uz cp - uy sp, uy uz cp + ux sp, -rho2 cp) + cth u
-                        const float rho2 = __fmaf_rn(ux, ux, uy * uy);
-                        const float k = __fsqrt_rn(__fdiv_rn(s2, rho2));
-                        const float bx = __fmaf_rn(ux * uz, cp, -(uy * sp));
-                        const float by = __fmaf_rn(uy * uz, cp, ux * sp);
-                        const float nx = __fmaf_rn(k, bx, ux * cth);
-                        const float ny = __fmaf_rn(k, by, uy * cth);
-                        const float nz = __fmaf_rn(-(k * cp), rho2, uz * cth);
-                        ux = nx; uy = ny; uz = nz;
-                    }
-                    tau = ismc_neglog_u32(r.w);
+            }
+            // spin (MLMC.py:181-198), computed by every lane of the walk and
+            // kept by those that interacted and survived the roulette
+            float sp, cp;
+            ismc_sincos_2pi(u2, &sp, &cp);
+            const float tnext = ismc_neglog_u32(r.w);
+            if (!stuck && !cross && !fin) {
+                ISMC_BRANCH(ISMC_BR_SPIN);
+                if (normal) {                               // MLMC.py:190-193
+                    ux = sq * cp;
+                    uy = sq * sp;
+                    uz = uz > 0.0f ? cth : -cth;
+                } else {                                    // MLMC.py:194-198
+                    // k = sin(theta)/sin(polar) = sq:
+                    //   new = k (ux uz cp - uy sp, uy uz cp + ux sp, -rho2 cp) + cth u
+                    const float bx = __fmaf_rn(ux * uz, cp, -(uy * sp));
+                    const float by = __fmaf_rn(uy * uz, cp, ux * sp);
+                    const float nx = __fmaf_rn(sq, bx, ux * cth);
+                    const float ny = __fmaf_rn(sq, by, uy * cth);
+                    const float nz = __fmaf_rn(-(sq * cp), rho2, uz * cth);
+                    ux = nx; uy = ny; uz = nz;
                 }
+                tau = tnext;
             }
         }
 
         // -------- a packet in front of a sphere port (ISMLMC.py:130-224, 239-340)
         if (to_sphere) {
+            ISMC_BRANCH(ISMC_BR_SPHERE);
             const float u1 = ismc_u01(r.y);
             if (c_exit >= I.cos_port[side]) {
                 bin = side ? ISMC_T_TU : ISMC_T_RS;
@@ -667,6 +732,7 @@ ismc_propagate_kernel(const PropParams P) {
         }
 
         if (fin) {
+            ISMC_BRANCH(ISMC_BR_FIN);
             unsigned long long* acc = ws->acc[slot];
             if (fin != 2) {
                 // weight absorbed so far is scored; a trapped packet's

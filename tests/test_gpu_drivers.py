@@ -144,8 +144,9 @@ def test_lookup_driver_cuda_path_gpu_tables(tmp_path):
              ("lookup", "input_distributions_samples"): 2}
     drv, ini, cp = _copy(tmp_path, "Lookup/lookup.py", edits)
     exe = os.path.join(ROOT, "ismc_gb300", "bin", "Lookup.o")
-    out = _run(drv, ["--gpu-tables", "--numpy-seed", "5", "--CUDA", "--CUDAsource", exe,
-                     "--GPU", "0", ini], os.path.dirname(drv))
+    # lookup.py's --GPU takes a list (nargs="*"): the configuration file goes first
+    out = _run(drv, ["--gpu-tables", "--numpy-seed", "5", "--CUDA", "--CUDAsource", exe, ini,
+                     "--GPU", "0"], os.path.dirname(drv))
     ma = re.search(r"mua = (\S+) \+/- (\S+) for R_d", out)
     ms = re.search(r"mus' = (\S+) \+/- (\S+) for R_d", out)
     assert ma and ms, out[-2000:]
