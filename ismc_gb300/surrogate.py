@@ -246,7 +246,8 @@ def objective_weights(meas, sigma, objective="chi2"):
 
 def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=10, verify_packets=1_000_000,
                     seed=7, fallback=True, correct=True, plain_packets=100_000, plain_max_evals=400,
-                    objective="chi2", anchor_packets=0, anchor_steps=5, test=None):
+                    objective="chi2", anchor_packets=0, anchor_steps=5, test=None,
+                    fallback_h0=0.15):
     """Solve many measurements [m x 3] of (R_d, T_d, T_u) with noise sigma (3,).
 
     (1) The surrogate on a 48 x 48 (ln mu_a, ln mu_s') grid proposes a start;
@@ -260,7 +261,8 @@ def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=10, 
     `correct`, a solve that fails the test is re-anchored at its point by that
     verification, re-solved and verified again.  (4) What still fails falls
     back to the plain path (PRAXIS on Monte Carlo), started from the
-    surrogate's answer.
+    surrogate's answer with PRAXIS's initial step `fallback_h0` (in ln units:
+    the answer is already close).
 
     Steps (1)-(3b) minimise `objective` (see objective_weights).  The test of
     step (3) is `test`: "fit" (the default for chi2) asks every verified value
@@ -317,10 +319,12 @@ def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=10, 
 
     def failed(V, VS, pred, pred_se):
         if test == "fit":
-            return np.any(np.abs(V - meas) > 3 * np.sqrt(sig ** 2 + VS ** 2), axis=1)
-        return np.any(np.abs(V - pred) > 3 * np.sqrt(VS ** 2 + pred_se ** 2), axis=1)
+            return np.abs(V - meas) > 3 * np.sqrt(sig ** 2 + VS ** 2)
+        return np.abs(V - pred) > 3 * np.sqrt(VS ** 2 + pred_se ** 2)
 
-    miss = failed(V, VS, pred, off_se)
+    fails = failed(V, VS, pred, off_se)          # [m x 3]: which of R_d, T_d, T_u failed
+    first_fails = fails.sum(0)
+    miss = fails.any(1)
     corrected = np.zeros(m, dtype=bool)
     # (3b) re-anchor the failures at their verified values, verify again
     t3 = time.perf_counter()
@@ -334,7 +338,7 @@ def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=10, 
         pred[idx] = predict(xi) + oi
         off_se[idx] = VS[idx]
         corrected[idx] = True
-        miss = failed(V, VS, pred, off_se)
+        miss = failed(V, VS, pred, off_se).any(1)
     T["correct_s"] = time.perf_counter() - t3
     # (4) fallback to the plain path for what still misses
     t4 = time.perf_counter()
@@ -345,7 +349,7 @@ def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=10, 
         reqs = [make_solve(sample_stack(1.0, 10.0, g, d, n), 1, sph, plain_packets,
                            (meas[i, 0], None, meas[i, 1], meas[i, 2]), x0=tuple(xr[i]),
                            seed=seed + 1, lo=(0.005, 0.5), hi=(20.0, 200.0),
-                           max_evals=plain_max_evals) for i in idx]
+                           max_evals=plain_max_evals, h0=fallback_h0) for i in idx]
         outp = engine.solve_batch(reqs)
         for i, o in zip(idx, outp):
             xr[i] = (o.x[0], o.x[1])
@@ -359,4 +363,5 @@ def surrogate_solve(sur, engine, meas, sigma, g=0.9, d=0.1, n=1.4, gn_steps=10, 
         (m + int(corrected.sum())) * verify_packets + fallback_evals * plain_packets
     return {"x": xr, "verified": V, "verified_se": VS, "corrected": corrected, "fallback": miss,
             "timing": T, "mc_packets": mc, "fallback_evals": fallback_evals,
-            "objective": objective, "test": test, "anchor_packets": anchor_packets}
+            "objective": objective, "test": test, "anchor_packets": anchor_packets,
+            "first_test_failures": first_fails.tolist()}
