@@ -564,6 +564,13 @@ def run_gpu(args, rank, world, dist):
                         useful_note="useful_frac = photon-steps/s x executed thread-instructions "
                                     "per step / (SMs x clock x 128): the issue-rate fraction "
                                     "with idle lanes of divergent instructions not counted")
+        if prof.get("algorithmic_inst_per_step"):
+            alg = float(prof["algorithmic_inst_per_step"])
+            roof.update(algorithmic_frac=steps_per_s * alg / (peak * 1e9),
+                        algorithmic_inst_per_step=alg,
+                        algorithmic_note="the building blocks a photon-step needs (Philox block, "
+                                         "spin, free path, its share of interface, incidence "
+                                         "and sphere work), per ncu counts of each block alone")
     else:
         roof.update(steps_per_s=steps_per_s)
     # the HBM side, for completeness: DRAM bytes per launch (ncu) over the launch

@@ -580,76 +580,36 @@ ismc_propagate_kernel(const PropParams P) {
             }
         } else {
             // -------- walk inside layer l (MLMC.py:95-200)
-            // A lane either reaches the next interface (reflect, refract or
-            // leave) or interacts inside the layer (hop, drop, roulette,
-            // spin).  In a warp both kinds nearly always occur together, so
-            // the two share one instruction stream: one division (the path to
-            // the boundary, or the Henyey-Greenstein quotient) and one square
-            // root (the refracted cosine, or sin(theta) / sin(polar)) serve
-            // both, and each lane keeps only its own results.  Every value is
-            // the same correctly rounded operation on the same operands as in
-            // a lane that computes one kind alone.
             ISMC_BRANCH(ISMC_BR_WALK);
             const int l = layer;
             const bool down = uz > 0.0f;
-            const uint32_t lf = I.ly[l].lflags;
-            const bool glass = (lf & ISMC_LF_GLASS) != 0u;
+            const bool glass = (I.ly[l].lflags & ISMC_LF_GLASS) != 0u;
             const float4 q0 = ismc_lq(I, l, 0);     // mut, inv_mut, drop, hgc
-            const float4 q1 = ismc_lq(I, l, 1);     // hgd, hge, hga, hgb
             const float4 q2 = ismc_lq(I, l, 2);     // z_top, z_bot, eta_up, eta_dn
             const float zb = down ? q2.y : q2.x;
             // distance to the boundary along z (rounding can leave z a hair outside)
             const float dist = fmaxf(down ? zb - z : z - zb, 0.0f);
             const float auz = fabsf(uz);
             const float mut = q0.x;
-            // a slide the packet cannot leave: give up on it
-            const bool stuck = glass && auz == 0.0f;
-            // free path tau/mut >= dist/|uz|, tested without a division
-            const bool cross = !stuck && (glass || (auz > 0.0f && dist * mut <= tau * auz));
-            const float u1 = ismc_u01(r.y), u2 = ismc_u01(r.z);
-            // the one division: dist / |uz| at an interface, the HG quotient
-            // (1 - g^2) / (1 - g + 2 g u1) in an interaction
-            const float quo = __fdiv_rn(cross ? dist : q0.w, cross ? auz : __fmaf_rn(q1.y, u1, q1.x));
-            // interface: refraction geometry (ismc_fresnel_reflects, split at its root)
-            const float eta = down ? q2.w : q2.z;
-            const float s2t = (eta * eta) * (1.0f - auz * auz);
-            const bool tir = s2t >= 1.0f;
-            // interaction: polar cosine, isotropic or Henyey-Greenstein (MLMC.py:183-186)
-            float cth = (lf & ISMC_LF_ISO) ? 2.0f * u1 - 1.0f
-                                           : fminf(fmaxf(q1.z * __fmaf_rn(-quo, quo, q1.w), -1.0f), 1.0f);
-            const float s2 = fmaxf(__fmaf_rn(-cth, cth, 1.0f), 0.0f);   // sin^2 theta
-            const bool normal = auz > 0.99999f;                          // MLMC.py:190
-            // rho2 = sin^2 of the polar angle from the transverse components
-            // (= 1 - uz^2 for a unit vector; this form keeps the FP32 norm error
-            // from growing as 1/(1 - uz^2))
-            const float rho2 = __fmaf_rn(ux, ux, uy * uy);
-            const float kk = __fdiv_rn(s2, rho2);
-            // the one square root
-            const float sq = __fsqrt_rn(cross ? (tir ? 0.0f : 1.0f - s2t) : (normal ? s2 : kk));
-            if (stuck) {
-                fin = 2;
-            } else if (cross) {
-                // ---- reach the interface
+            if (glass && auz == 0.0f) {
+                fin = 2;                                   // cannot leave a slide: give up on it
+            } else if (glass || (auz > 0.0f && dist * mut <= tau * auz)) {
+                // ---- reach the interface (free path tau/mut >= dist/|uz|, no division)
                 ISMC_BRANCH(ISMC_BR_INTERFACE);
                 if (!glass) {
-                    tau = fmaxf(__fmaf_rn(-quo, mut, tau), 0.0f);
+                    const float d = __fdiv_rn(dist, auz);
+                    tau = fmaxf(__fmaf_rn(-d, mut, tau), 0.0f);
                 } else if (!compat && q0.z > 0.0f) {
-                    const float wn = w * ismc_expneg(q0.z * quo);
+                    const float d = __fdiv_rn(dist, auz);
+                    const float wn = w * ismc_expneg(q0.z * d);
                     absorbed = absorbed + (w - wn);
                     w = wn;
                 }
                 z = zb;
                 const int nl = down ? l + 1 : l - 1;
-                // reflect-or-transmit draw without the Fresnel division (ismc_fresnel_reflects)
-                bool refl = tir;
-                if (!tir) {
-                    const float a = eta * auz, b = eta * sq;
-                    const float rsn = a - sq, rsd = a + sq, rpn = b - auz, rpd = b + auz;
-                    const float x = rsn * rpd, y = rpn * rsd, den = rsd * rpd;
-                    refl = u0 * (den * den) < 0.5f * __fmaf_rn(x, x, y * y);
-                }
-                const float ct = tir ? 0.0f : sq;
-                if (refl) {
+                const float eta = down ? q2.w : q2.z;
+                float ct;
+                if (ismc_fresnel_reflects(eta, auz, u0, &ct)) {
                     uz = -uz;
                 } else if (nl < 0 || nl >= (int)L) {
                     side = nl < 0 ? 0u : 1u;
@@ -679,29 +639,43 @@ ismc_propagate_kernel(const PropParams P) {
                     if (u0 < I.roul_inv_m) w = w * I.roul_m;
                     else { w = 0.0f; fin = 1; }
                 }
-            }
-            // spin (MLMC.py:181-198), computed by every lane of the walk and
-            // kept by those that interacted and survived the roulette
-            float sp, cp;
-            ismc_sincos_2pi(u2, &sp, &cp);
-            const float tnext = ismc_neglog_u32(r.w);
-            if (!stuck && !cross && !fin) {
-                ISMC_BRANCH(ISMC_BR_SPIN);
-                if (normal) {                               // MLMC.py:190-193
-                    ux = sq * cp;
-                    uy = sq * sp;
-                    uz = uz > 0.0f ? cth : -cth;
-                } else {                                    // MLMC.py:194-198
-                    // k = sin(theta)/sin(polar) = sq:
-                    //   new = k (ux uz cp - uy sp, uy uz cp + ux sp, -rho2 cp) + cth u
-                    const float bx = __fmaf_rn(ux * uz, cp, -(uy * sp));
-                    const float by = __fmaf_rn(uy * uz, cp, ux * sp);
-                    const float nx = __fmaf_rn(sq, bx, ux * cth);
-                    const float ny = __fmaf_rn(sq, by, uy * cth);
-                    const float nz = __fmaf_rn(-(sq * cp), rho2, uz * cth);
-                    ux = nx; uy = ny; uz = nz;
+                if (!fin) {
+                    ISMC_BRANCH(ISMC_BR_SPIN);
+                    const float u1 = ismc_u01(r.y), u2 = ismc_u01(r.z);
+                    float cth;
+                    if (I.ly[l].lflags & ISMC_LF_ISO) {
+                        cth = 2.0f * u1 - 1.0f;
+                    } else {
+                        const float4 q1 = ismc_lq(I, l, 1);     // hgd, hge, hga, hgb
+                        const float t = __fdiv_rn(q0.w, __fmaf_rn(q1.y, u1, q1.x));
+                        cth = q1.z * __fmaf_rn(-t, t, q1.w);
+                        cth = fminf(fmaxf(cth, -1.0f), 1.0f);
+                    }
+                    float sp, cp;
+                    ismc_sincos_2pi(u2, &sp, &cp);
+                    const float s2 = fmaxf(__fmaf_rn(-cth, cth, 1.0f), 0.0f);   // sin^2 theta
+                    if (fabsf(uz) > 0.99999f) {             // MLMC.py:190-193
+                        const float sth = __fsqrt_rn(s2);
+                        ux = sth * cp;
+                        uy = sth * sp;
+                        uz = uz > 0.0f ? cth : -cth;
+                    } else {                                 // MLMC.py:194-198
+                        // rho2 = sin^2 of the polar angle from the transverse
+                        // components (= 1 - uz^2 for a unit vector; this form keeps
+                        // the FP32 norm error from growing as 1/(1 - uz^2)), and
+                        // k = sin(theta)/sin(polar) from one division and one root:
+                        //   new = k (ux uz cp - uy sp, uy uz cp + ux sp, -rho2 cp) + cth u
+                        const float rho2 = __fmaf_rn(ux, ux, uy * uy);
+                        const float k = __fsqrt_rn(__fdiv_rn(s2, rho2));
+                        const float bx = __fmaf_rn(ux * uz, cp, -(uy * sp));
+                        const float by = __fmaf_rn(uy * uz, cp, ux * sp);
+                        const float nx = __fmaf_rn(k, bx, ux * cth);
+                        const float ny = __fmaf_rn(k, by, uy * cth);
+                        const float nz = __fmaf_rn(-(k * cp), rho2, uz * cth);
+                        ux = nx; uy = ny; uz = nz;
+                    }
+                    tau = ismc_neglog_u32(r.w);
                 }
-                tau = tnext;
             }
         }
 
