@@ -82,3 +82,40 @@ def test_grid_instances_are_byte_identical_to_the_loop():
             for a, b in zip(arr, ref):
                 assert bytes(a) == bytes(b)
             assert index["i"].max() == 4 and index["j"].max() == 3 and index["r"].max() == runs - 1
+
+
+def test_component_costs_from_an_ncu_csv(tmp_path):
+    """ismc_gb300.perf turns an ncu CSV of the building-block kernels into
+    warp instructions per call, with the shared loop's overhead subtracted."""
+    from ismc_gb300 import perf
+    warps_calls = perf._WARPS * perf._ITERS
+    hdr = ('"ID","Process ID","Process Name","Host Name","Kernel Name","Context","Stream",'
+           '"Block Size","Grid Size","Device","CC","Section Name","Metric Name","Metric Unit",'
+           '"Metric Value"')
+
+    def row(i, k, m, v):
+        return (f'"{i}","1","components","h","{k}(float *, unsigned int)","1","7","(256, 1, 1)",'
+                f'"(608, 1, 1)","0","10.3","Command line profiler metrics","{m}","inst","{v}"')
+    lines = ["==PROF== Connected", hdr,
+             row(0, "k_loop", "smsp__inst_executed.sum", int(3.25 * warps_calls)),
+             row(0, "k_loop", "smsp__thread_inst_executed.sum", int(3.25 * warps_calls * 32)),
+             row(1, "k_div", "smsp__inst_executed.sum", int(16.25 * warps_calls)),
+             row(1, "k_div", "smsp__thread_inst_executed.sum", int(16.25 * warps_calls * 30))]
+    p = tmp_path / "c.csv"
+    p.write_text("\n".join(lines) + "\n")
+    got = perf.components_from_csv(str(p))
+    assert abs(got["div"]["warp_inst_per_call"] - 13.0) < 1e-9
+    assert abs(got["div"]["lanes"] - 30.0) < 1e-9
+    assert abs(got["_loop_overhead"] - 3.25) < 1e-9
+
+
+def test_reference_cuda_arm_refuses_stacks_with_slides(capsys):
+    """The reference kernel is timed only on slide-less stacks: on a stack with
+    slides the arm prints its unavailable line and runs nothing."""
+    import argparse
+    import json
+    import bench
+    bench.run_refcuda(argparse.Namespace(stack="bench1", packets=10**8, steps=1, warmup=1), 0)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["workload"] == "refcuda"
+    assert "slides" in line["unavailable"]
