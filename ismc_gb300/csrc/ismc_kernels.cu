@@ -327,22 +327,9 @@ __global__ void __launch_bounds__(1024) ismc_scan_kernel(unsigned long long* pre
 //             (Fresnel reflect / refract / exit into a sphere) or interacts
 //             inside the layer (hop, drop, roulette, spin, next free path).
 // ============================================================================
-// A warp's queue position: uniform across its lanes, used only while the warp
-// hands out packets (about one iteration in five), so it is kept here between
-// hand-outs instead of in every lane's registers through the event code.
-struct WarpQueue {
-    unsigned long long c_next, c_end;   // packet id range left in the current chunk
-    unsigned long long p_next, p_end;   // the claimed chunk not yet placed
-    int s_inst[2];                      // instance held by slot 0 / 1
-    int cur;                            // slot packets are handed out from
-    int pend;                           // instance of the claimed chunk, -1 = none
-    int qdone;                          // the queue is empty
-    int _pad[3];
-};
 struct WarpSlots {
     DevInst slot[2];
     unsigned long long acc[2][ISMC_NACC];
-    WarpQueue q;
 };
 // the round keys are read as 16-byte words from every slot of every warp
 static_assert(offsetof(DevInst, rk) % 16 == 0, "DevInst::rk alignment");
@@ -433,18 +420,18 @@ ismc_propagate_kernel(const PropParams P) {
     extern __shared__ __align__(16) unsigned char ismc_smem[];
     const int lane = threadIdx.x & 31;
     WarpSlots* ws = reinterpret_cast<WarpSlots*>(ismc_smem) + (threadIdx.x >> 5);
-    WarpQueue* const q = &ws->q;
     if (lane < 2 * ISMC_NACC) (&ws->acc[0][0])[lane] = 0ull;
-    if (lane == 0) {
-        q->c_next = q->c_end = q->p_next = q->p_end = 0ull;
-        q->s_inst[0] = q->s_inst[1] = -1;
-        q->cur = 0;
-        q->pend = -1;
-        q->qdone = 0;
-    }
     __syncwarp();
     const unsigned long long n_chunks = P.chunk_prefix[P.n_inst];
     const unsigned lt_mask = (1u << lane) - 1u;
+
+    // ---- warp-uniform queue state
+    int s_inst0 = -1, s_inst1 = -1;      // instance held by slot 0 / 1
+    int cur = 0;                          // slot packets are handed out from
+    unsigned long long c_next = 0, c_end = 0;   // packet id range left in the current chunk
+    int pend = -1;                        // claimed chunk not yet placed
+    unsigned long long p_next = 0, p_end = 0;
+    bool qdone = false;
 
     // ---- lane state
     bool alive = false;
@@ -462,11 +449,6 @@ ismc_propagate_kernel(const PropParams P) {
         ISMC_BRANCH(ISMC_BR_ITER);
         if (need) {     // every lane busy (the common case): nothing to hand out
             ISMC_BRANCH(ISMC_BR_HANDOUT);
-            // the warp's queue position, in registers for this hand-out only
-            int s_inst0 = q->s_inst[0], s_inst1 = q->s_inst[1], cur = q->cur, pend = q->pend;
-            unsigned long long c_next = q->c_next, c_end = q->c_end;
-            unsigned long long p_next = q->p_next, p_end = q->p_end;
-            bool qdone = q->qdone != 0;
             while (need) {
                 if (c_next < c_end) {
                     const unsigned long long avail = c_end - c_next;
@@ -542,14 +524,6 @@ ismc_propagate_kernel(const PropParams P) {
                 if (tgt) s_inst1 = pend; else s_inst0 = pend;
                 cur = tgt; c_next = p_next; c_end = p_end; pend = -1;
             }
-            // every lane holds the same values: one lane writes them back
-            __syncwarp();
-            if (lane == 0) {
-                q->c_next = c_next; q->c_end = c_end; q->p_next = p_next; q->p_end = p_end;
-                q->s_inst[0] = s_inst0; q->s_inst[1] = s_inst1;
-                q->cur = cur; q->pend = pend; q->qdone = qdone ? 1 : 0;
-            }
-            __syncwarp();
             if (!__any_sync(ISMC_FULL, alive)) {
                 if (qdone && pend < 0) break;
                 continue;
@@ -746,7 +720,7 @@ ismc_propagate_kernel(const PropParams P) {
                 if (fin == 3) atomicAdd(acc + 14, 1ull);
             } else {
                 atomicAdd(acc + 13, 1ull);
-                atomicMin(&P.tally[q->s_inst[slot]].status, ISMC_ERR_STEP_LIMIT);
+                atomicMin(&P.tally[slot ? s_inst1 : s_inst0].status, ISMC_ERR_STEP_LIMIT);
             }
             lev += ev;
             if ((lev | lsteps) >= 0x80000000u) ismc_flush_counts(acc, lsteps, lev, lreinc);
@@ -756,9 +730,8 @@ ismc_propagate_kernel(const PropParams P) {
     __syncwarp();
     ismc_flush_counts(ws->acc[lslot], lsteps, lev, lreinc);
     __syncwarp();
-    const int inst0 = q->s_inst[0], inst1 = q->s_inst[1];
-    ismc_flush_slot(ws, 0, inst0, P.tally, lane);
-    ismc_flush_slot(ws, 1, inst1, P.tally, lane);
+    ismc_flush_slot(ws, 0, s_inst0, P.tally, lane);
+    ismc_flush_slot(ws, 1, s_inst1, P.tally, lane);
 }
 
 // ============================================================================
