@@ -4,7 +4,7 @@
 #include <stdint.h>
 #include "../../include/ismc.h"
 
-#define ISMC_HDR_WORDS 40
+#define ISMC_HDR_WORDS 44
 #define ISMC_LAYER_FIELDS 16
 
 // Layer flags
@@ -29,7 +29,7 @@ struct DevLayer {
 static_assert(sizeof(DevLayer) == 64, "DevLayer layout");
 
 // Prepared instance: everything the walk needs, derived once per launch by
-// ismc_prepare_kernel: a 40-word header, then one DevLayer per layer.  One
+// ismc_prepare_kernel: a 44-word header, then one DevLayer per layer.  One
 // warp copies it word by word into its shared-memory slot.
 struct DevInst {
     // header: 40 words
@@ -47,6 +47,11 @@ struct DevInst {
     // (rk[2r], rk[2r+1]) = (seed_lo + r W0, seed_hi + r W1) mod 2^32, read as
     // five 16-byte words (byte offset 80, 16-byte aligned)
     uint32_t rk[20];
+    // the launch's incidence, the same for every packet of the instance: the
+    // reflection probability and refracted cosine the incidence event would
+    // compute for the launch direction (same operations, so the same bits)
+    float launch_R, launch_ct;
+    uint32_t _hpad2[2];
     DevLayer ly[ISMC_MAXL];     // per-layer constants, 64 B each
 };
 

@@ -189,6 +189,20 @@ __global__ void ismc_prepare_kernel(const ismc_instance* __restrict__ in, uint32
     D.t_tot = z;
     D.eta_in[0] = __fdiv_rn(1.0f, S.n[0 < L ? 0 : 0]);
     D.eta_in[1] = __fdiv_rn(1.0f, S.n[L - 1]);
+    // the launch's incidence on the top face, as the incidence event computes it
+    {
+        float ct;
+        float R = ismc_fresnel(D.eta_in[0], fabsf(D.uz0), &ct);
+        if (I.mode == ISMC_MODE_COMPAT && (D.ly[0].lflags & ISMC_LF_GLASS)) {
+            float ct2;
+            const float r2 = ismc_fresnel(D.ly[0].eta_dn, fabsf(D.uz0), &ct2);
+            const float om = 1.0f - R;
+            R = R + __fdiv_rn((om * om) * r2, 1.0f - R * r2);
+        }
+        D.launch_R = R;
+        D.launch_ct = ct;
+        D._hpad2[0] = D._hpad2[1] = 0u;
+    }
     out[i] = D;
 
     // ---------------------------------------------------------------- analytic
@@ -554,16 +568,23 @@ ismc_propagate_kernel(const PropParams P) {
             const int l = top ? 0 : (int)L - 1;
             const float c = fabsf(uz);
             const float eta = I.eta_in[top ? 0 : 1];
-            float ct;
-            float R = ismc_fresnel(eta, c, &ct);
             const bool lglass = (I.ly[l].lflags & ISMC_LF_GLASS) != 0u;
-            if (compat && lglass) {
-                // slide on the incidence face: two-interface series with the
-                // ambient-side cosine for both interfaces (ISMLMC.py:81-91)
-                float ct2;
-                const float r2 = ismc_fresnel(top ? I.ly[l].eta_dn : I.ly[l].eta_up, c, &ct2);
-                const float om = 1.0f - R;
-                R = R + __fdiv_rn((om * om) * r2, 1.0f - R * r2);
+            float ct, R;
+            if (ev == 1u) {
+                // the launch (the packet's first event): the instance's
+                // precomputed values, the same bits as computed here
+                R = I.launch_R;
+                ct = I.launch_ct;
+            } else {
+                R = ismc_fresnel(eta, c, &ct);
+                if (compat && lglass) {
+                    // slide on the incidence face: two-interface series with the
+                    // ambient-side cosine for both interfaces (ISMLMC.py:81-91)
+                    float ct2;
+                    const float r2 = ismc_fresnel(top ? I.ly[l].eta_dn : I.ly[l].eta_up, c, &ct2);
+                    const float om = 1.0f - R;
+                    R = R + __fdiv_rn((om * om) * r2, 1.0f - R * r2);
+                }
             }
             if (u0 < R) {
                 to_sphere = true;
