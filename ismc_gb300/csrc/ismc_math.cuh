@@ -106,9 +106,7 @@ __device__ __forceinline__ float ismc_neglog_u32(uint32_t x) {
     p = __fmaf_rn(f, p, 0.333333284f);
     const float f2 = f * f;
     const float lnm = __fmaf_rn(f2, __fmaf_rn(f, p, -0.5f), f);
-    // e in [-32, 0] as a float, exactly, without a conversion instruction:
-    // (1.5 * 2^23 + e) - 1.5 * 2^23
-    const float fe = __int_as_float(0x4B400000 + e) - 12582912.0f;
+    const float fe = (float)e;
     // ln2 split so that fe * LN2_HI is exact for |e| < 2^8
     const float ln = __fmaf_rn(fe, 0.693145752f, __fmaf_rn(fe, 1.42860677e-06f, lnm));
     return -ln;
@@ -121,9 +119,7 @@ __device__ __forceinline__ void ismc_sincos_2pi(float u, float* s, float* c) {
     const float v = 4.0f * u;
     const float qf = rintf(v);
     const float r = v - qf;
-    // qf is an integer in [0, 4]: adding 2^23 places it in the low mantissa
-    // bits exactly, which gives the quadrant without a conversion instruction
-    const int q = __float_as_int(qf + 8388608.0f) & 3;
+    const int q = ((int)qf) & 3;
     const float r2 = r * r;
     // (pi/2)^k / k! with alternating signs
     float sp = __fmaf_rn(r2, 1.60441184e-04f, -4.68175413e-03f);   // +(pi/2)^9/9!, -(pi/2)^7/7!
