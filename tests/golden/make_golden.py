@@ -107,6 +107,18 @@ CASES = {
                                     layer(1.50, 1.0, 20.0, 0.0, 0.03),
                                     layer(1.36, 0.5, 60.0, 0.9, 0.12),
                                     GLASS15], spheres(), 200000, 64, 3900),
+    # the multilayer benchmark stack with the 8-degree launch (specular_included):
+    # the tilted launch through the slide's two-interface series
+    "bench1_specular_included": ("ISMLMC", [GLASS152,
+                                            layer(1.37, 0.5, 200.0, 0.8, 0.01),
+                                            layer(1.40, 2.0, 120.0, 0.9, 0.15),
+                                            layer(1.44, 0.2, 50.0, 0.75, 0.3),
+                                            GLASS152], spheres(specular_included=True),
+                                 400000, 64, 4100),
+    # the single-layer benchmark stack with no spheres: acceptance by angle
+    # (ISMLMC.py:163, 211, 273, 325) behind slides
+    "bench0_no_spheres": ("ISMLMC", [GLASS15, SLAB0, GLASS15], spheres(R=False, T=False),
+                          400000, 64, 4200),
     # tissue directly against ambient on both faces, both spheres, thicker slab
     "bare_two_layer": ("ISMLMC", [layer(1.4, 0.5, 50.0, 0.85, 0.1),
                                   layer(1.33, 0.2, 30.0, 0.7, 0.2)], spheres(), 400000, 64, 4000),
