@@ -27,6 +27,9 @@ bounded packet sample of the same workload.
 Reference CUDA arm (--impl reference --workload refcuda): the reference's own
 CUDA kernel and host entry point (CUDA/CUDAISMLMC.h, compiled unmodified from a
 staged copy by oracle/build_ref.py) on the same GPU, in calls of 1e7 packets.
+Reference Python arm (--impl reference --workload refpython): the reference's
+own ISMLMC.py / MLMC.py (staged unmodified by oracle/build_ref.py) on every host
+core, one spawned process per core, each step a bounded packet sample.
 """
 import argparse
 import ctypes as C
@@ -375,6 +378,59 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_refpython(args, rank):
+    """The reference's own Python forward model on every host core (--impl
+    reference --workload refpython): ISMLMC() of the unmodified ISMLMC.py /
+    MLMC.py that oracle/build_ref.py stages, one spawned process per core, each
+    step a bounded packet sample of the chosen stack (oracle/refpython.py)."""
+    if rank != 0:
+        return
+    st = args.stack
+    base = {"impl": "reference", "workload": "refpython", "metric": "photons/s",
+            "unit": "photons/s", "config": workload_config(st, args.packets)}
+    from oracle import build_ref, refpython
+    model = build_ref.staged_python()
+    if not model:
+        print(json.dumps(dict(base, unavailable="the reference's Python model was not staged into "
+                              "oracle/_ref/python (oracle/build_ref.py stage())")), flush=True)
+        return
+    procs = os.cpu_count()
+    layers = refpython.layer_tuples(workload_layers(st))
+    sph = refpython.sphere_dict(workload_spheres())
+    with refpython.Runner(model, procs) as pool:
+        # start the workers, then size one step to about 8 s of every core's
+        # time from the CPU seconds of a probe
+        pool.run(layers, sph, 10, SEED)
+        probe = 500
+        for w in range(max(args.warmup, 1)):
+            _, _, c = pool.run(layers, sph, probe, SEED + 1000 * (w + 1))
+        per_worker = max(probe, int(probe * 8.0 * procs / max(c, 1e-3)))
+        times, cpu, sums = [], 0.0, [0.0] * 5
+        for k in range(args.steps):
+            tallies, wall, c = pool.run(layers, sph, per_worker, SEED + 100000 * (k + 1))
+            times.append(wall)
+            cpu += c
+            sums = [a + b for a, b in zip(sums, tallies)]
+    total = sum(times)
+    per_step = per_worker * procs
+    value = per_step * args.steps / total
+    line = dict(base, value=value, n_gpus=1, steps=args.steps, warmup=args.warmup,
+                ms_per_step=1000 * total / args.steps, higher_is_better=True, scaling="weak",
+                vs_baseline=None, dtype="f64", data="synthetic",
+                config=dict(base["config"], packets_per_step=per_step,
+                            note="each step is a bounded packet sample of the workload"),
+                cpu_baseline={"value": value, "unit": "photons/s", "cores": procs,
+                              "kind": "reference",
+                              "sample": f"{per_step} packets per step ({per_worker} on each of "
+                                        f"{procs} processes), the reference's ISMLMC.py"},
+                e2e={"value": value, "unit": "photons/s", "h2d_bytes_per_step": 0,
+                     "d2h_bytes_per_step": 0},
+                result={"tallies": ["A", "R_d", "R_s", "T_d", "T_u"],
+                        "mean": [v / args.steps for v in sums],
+                        "photons_per_cpu_second": per_step * args.steps / max(cpu, 1e-9)})
+    print(json.dumps(line), flush=True)
+
+
 def run_refcuda(args, rank):
     """The reference's own CUDA forward model on this GPU (--impl reference
     --workload refcuda): kernel CUDAISMLMC timed alone with CUDA events, and the
@@ -695,7 +751,7 @@ def main():
     ap.add_argument("--packets", type=int, default=PACKETS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["forward", "lookup", "tables", "surrogate", "solve",
-                                           "dropin", "train", "refcuda"],
+                                           "dropin", "train", "refcuda", "refpython"],
                     default="forward")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="size factor for the secondary workloads (1 = full benchmark size)")
@@ -715,6 +771,11 @@ def main():
         if args.impl != "reference":
             ap.error("--workload refcuda is the reference CUDA arm: use --impl reference")
         run_refcuda(args, rank)
+        return
+    if args.workload == "refpython":
+        if args.impl != "reference":
+            ap.error("--workload refpython is a reference arm: use --impl reference")
+        run_refpython(args, rank)
         return
     if args.workload != "forward":
         if rank == 0 and args.impl == "gpu":

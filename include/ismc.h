@@ -266,6 +266,14 @@ typedef struct ismc_solve_req {
     uint32_t fresh_streams;   /* 0: every evaluation of a solve reuses its Philox stream (common
                                  random numbers, a deterministic objective); 1: a new stream per
                                  evaluation, like the reference's global random state */
+    uint32_t max_refits;      /* re-runs of a minimisation that stopped short (0: none).  PRAXIS
+                                 stops after two iterations without progress, which a rough
+                                 Monte Carlo objective can cause far from the minimum.  An end
+                                 point inside the box whose cost exceeds 5x the objective's own
+                                 Monte Carlo standard error is probed 3 % either side along each
+                                 axis; a probe 10 % lower starts a re-run from it.  Not for
+                                 minimisations stopped by max_evals. */
+    uint32_t _pad0;
     double meas[4];           /* measured R_d, R_s, T_d, T_u; NaN = not measured */
     double x0[2];             /* initial (mu_a, mu_s') */
     double lo[2], hi[2];      /* accepted box for (mu_a, mu_s'): answers outside it are
@@ -281,6 +289,8 @@ typedef struct ismc_solve_out {
     uint32_t restarts;
     int32_t status;           /* ISMC_OK, or ISMC_ERR_CAPACITY when every restart left the box */
     uint32_t rounds;          /* batched launches this solve took part in */
+    uint32_t refits;          /* re-runs after a minimisation stopped short (max_refits) */
+    uint32_t _pad0;
 } ismc_solve_out;
 
 /* Solve n independent inverse problems; out has n entries. */

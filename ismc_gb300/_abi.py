@@ -65,13 +65,15 @@ class SolveReq(C.Structure):
     _fields_ = [("base", Instance), ("layer", C.c_uint32), ("separate", C.c_uint32),
                 ("log_coords", C.c_uint32), ("max_evals", C.c_uint32),
                 ("max_restarts", C.c_uint32), ("fresh_streams", C.c_uint32),
+                ("max_refits", C.c_uint32), ("_pad0", C.c_uint32),
                 ("meas", C.c_double * 4), ("x0", C.c_double * 2), ("lo", C.c_double * 2),
                 ("hi", C.c_double * 2), ("h0", C.c_double), ("t0", C.c_double)]
 
 
 class SolveOut(C.Structure):
     _fields_ = [("x", C.c_double * 2), ("cost", C.c_double), ("evals", C.c_uint32),
-                ("restarts", C.c_uint32), ("status", C.c_int32), ("rounds", C.c_uint32)]
+                ("restarts", C.c_uint32), ("status", C.c_int32), ("rounds", C.c_uint32),
+                ("refits", C.c_uint32), ("_pad0", C.c_uint32)]
 
 
 OBJECTIVE = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_int, C.c_void_p)

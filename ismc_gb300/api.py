@@ -285,7 +285,8 @@ def slab_instances(mua, mus_reduced, g, d, n, spheres: Spheres, n_packets, seed:
 def make_solve(layers: Sequence[Layer], layer: int, spheres: Spheres, n_packets: int,
                meas, x0, lo=(1e-6, 1e-6), hi=(1e6, 1e6), seed: int = 0, separate=False,
                log_coords=True, h0=None, t0=None, max_evals=400, max_restarts=3,
-               mode="compat", roulette_threshold=1e-4, fresh_streams=False) -> _abi.SolveReq:
+               mode="compat", roulette_threshold=1e-4, fresh_streams=False,
+               max_refits=2) -> _abi.SolveReq:
     """One plain-path inverse problem: find (mu_a, mu_s') of `layer` so that the
     simulated (R_d, R_s, T_d, T_u) match `meas` (None = not measured) under the
     reference's cost (minimization.py:231-238).  In log coordinates the PRAXIS
@@ -294,7 +295,9 @@ def make_solve(layers: Sequence[Layer], layer: int, spheres: Spheres, n_packets:
     fresh_streams=False gives every evaluation of one solve the same Philox
     stream (common random numbers: the objective is then a deterministic
     function of the parameters); True draws a new stream per evaluation, as the
-    reference's global random state does."""
+    reference's global random state does.  max_refits: how many times a
+    minimisation that ended far above the objective's Monte Carlo noise is run
+    again from where it ended (ismc_solve_req.max_refits)."""
     r = _abi.SolveReq()
     r.base = make_instance(layers, spheres, n_packets, seed=seed, mode=mode,
                            roulette_threshold=roulette_threshold)
@@ -304,6 +307,7 @@ def make_solve(layers: Sequence[Layer], layer: int, spheres: Spheres, n_packets:
     r.max_evals = int(max_evals)
     r.max_restarts = int(max_restarts)
     r.fresh_streams = 1 if fresh_streams else 0
+    r.max_refits = int(max_refits)
     for k in range(4):
         r.meas[k] = float("nan") if meas[k] is None else float(meas[k])
     r.x0[0], r.x0[1] = float(x0[0]), float(x0[1])

@@ -114,6 +114,7 @@ int main(int argc, char** argv) {
         q.log_coords = 0;
         q.max_evals = (uint32_t)max_evals;
         q.max_restarts = 20;         // the reference repeats until inside, unbounded
+        q.max_refits = 2;
         q.fresh_streams = crn ? 0 : 1;
         q.meas[0] = Rd; q.meas[1] = Rs; q.meas[2] = Td; q.meas[3] = Tu;
         q.x0[0] = mua0; q.x0[1] = mus0;

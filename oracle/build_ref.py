@@ -15,6 +15,11 @@
                                  (Lookup/lookup.py, Minimization/minimization.py,
                                  */example.ini), staged the same way for the
                                  end-to-end driver tests on the GPU machine
+  oracle/_ref/python/            byte-for-byte copies of the reference's Python
+                                 forward model (ISMLMC.py, MLMC.py), staged the
+                                 same way, so that the reference itself can be
+                                 timed on the GPU machine's host cores
+                                 (oracle/refpython.py)
   oracle/_ref/refcuda_bench      oracle/refcuda_bench.cu, the project's timing
                                  harness, compiled against the staged header
                                  for sm_103a (build_refcuda(), on the GPU
@@ -40,6 +45,10 @@ STAGED = ("CUDA/CUDAISMLMC.h",)
 DRIVERS = ("Lookup/lookup.py", "Lookup/example.ini", "Minimization/minimization.py",
            "Minimization/example.ini")
 DRIVERS_DIR = os.path.join(OUT, "drivers")
+# the reference's Python forward model: ISMLMC() (ISMLMC.py:101-347) and the
+# multilayer walk it calls (MLMC.py:283-409); it imports only math and random
+PYTHON_MODEL = ("ISMLMC.py", "MLMC.py")
+PYTHON_DIR = os.path.join(OUT, "python")
 HARNESS = os.path.join(HERE, "refcuda_bench.cu")
 REFCUDA_BIN = os.path.join(OUT, "refcuda_bench")
 
@@ -56,13 +65,15 @@ def _sha(path):
 
 
 def stage():
-    """Copy the reference's CUDA forward model, unmodified, into oracle/_ref/src/.
+    """Copy the reference's CUDA forward model, its driver scripts and its
+    Python forward model, unmodified, into oracle/_ref/ (src/, drivers/, python/).
     Returns the staged header's path, or None when neither the checkout nor an
     earlier staged copy exists."""
     ref = reference_dir()
     if ref:
         copies = [(rel, os.path.join(SRC, os.path.basename(rel))) for rel in STAGED]
         copies += [(rel, os.path.join(DRIVERS_DIR, rel)) for rel in DRIVERS]
+        copies += [(rel, os.path.join(PYTHON_DIR, rel)) for rel in PYTHON_MODEL]
         for rel, dst in copies:
             src = os.path.join(ref, rel)
             os.makedirs(os.path.dirname(dst), exist_ok=True)
@@ -78,6 +89,14 @@ def staged_driver(rel):
     stage()
     p = os.path.join(DRIVERS_DIR, rel)
     return p if os.path.exists(p) else None
+
+
+def staged_python():
+    """Directory holding the staged ISMLMC.py / MLMC.py, or None where they
+    were never staged."""
+    stage()
+    ok = all(os.path.exists(os.path.join(PYTHON_DIR, f)) for f in PYTHON_MODEL)
+    return PYTHON_DIR if ok else None
 
 
 def build_praxis():

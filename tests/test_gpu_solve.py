@@ -53,3 +53,63 @@ def test_minimize_distribution_outer_loop(engine):
     assert np.all(np.abs(res["mu_s_per_sample"] / truth[1] - 1) < 0.10), res["mu_s_per_sample"]
     assert abs(res["mu_s"] / truth[1] - 1) < 0.06
     assert res["mu_a_unc"] >= 0 and res["mu_s_unc"] >= 0
+
+
+def test_refit_when_a_fit_stopped_short(engine):
+    """PRAXIS can end a minimisation of a Monte Carlo objective far from its
+    minimum.  64 solves of one measurement from one start (the single-slab
+    stack between slides, 2e5 packets per objective, common random numbers):
+    without refits some end with residuals of several percent, most near
+    0.02 %; with them (ismc_solve_req.max_refits) every fit that stopped short
+    is probed, re-run and lands near the truth."""
+    import numpy as np
+    sph = bench_spheres()
+    truth = (0.8, 25.0)
+    m = engine.run_batch([make_instance(_stack(*truth), sph, 4_000_000, seed=31)])[0]
+    meas = (m["R_d"], None, m["T_d"], m["T_u"])
+
+    def solve(max_refits):
+        return engine.solve_batch([make_solve(_stack(1.0, 20.0), 1, sph, 200_000, meas,
+                                              x0=(1.0, 20.0), lo=(0.05, 2.0), hi=(10.0, 200.0),
+                                              seed=i, max_evals=300, max_refits=max_refits)
+                                   for i in range(64)])
+
+    plain, refit = solve(0), solve(2)
+    err = lambda out: np.array([[abs(o.x[0] / truth[0] - 1), abs(o.x[1] / truth[1] - 1)]
+                                for o in out])
+    e0, e2 = err(plain), err(refit)
+    assert all(o.status == 0 for o in plain + refit)
+    assert all(o.refits == 0 for o in plain)
+    # residuals of 5 % or more: ten times the cost's Monte Carlo noise
+    short = [k for k, o in enumerate(plain) if o.cost > 0.05]
+    assert short, "no fit stopped short"
+    for k in short:
+        assert refit[k].refits >= 1 and refit[k].cost < plain[k].cost, k
+    assert e0[:, 1].max() > 0.05
+    assert e2.max(axis=0)[1] < 0.04, e2.max(axis=0)
+    # fits that ended at their minimum are left alone (or only probed)
+    for k, o in enumerate(plain):
+        if o.cost < 0.002:
+            assert refit[k].refits == 0 and list(refit[k].x) == list(o.x), k
+
+
+def test_probes_leave_a_measurement_limited_fit_alone(engine):
+    """An unreachable unscattered transmittance leaves a residual no
+    (mu_a, mu_s') removes.  The fit ends far above the Monte Carlo noise, so it
+    is probed (four evaluations 3 % either side of the end point), but no probe
+    is 10 % lower: no refit, the same answer, four more evaluations."""
+    sph = bench_spheres()
+    m = engine.run_batch([make_instance(_stack(0.8, 25.0), sph, 4_000_000, seed=41)])[0]
+    meas = (m["R_d"], None, m["T_d"], 0.1)
+    kw = dict(x0=(1.0, 20.0), lo=(0.05, 2.0), hi=(10.0, 200.0), seed=9, max_evals=300)
+    # one solve per call: the Philox stream of a solve follows its index in the
+    # batch, so both calls minimise the same objective
+    one, probed = (engine.solve_batch([make_solve(_stack(1.0, 20.0), 1, sph, 200_000, meas,
+                                                  max_refits=n, **kw)])[0] for n in (0, 2))
+    assert one.status == 0 and probed.status == 0
+    # the T_u term alone leaves |0.1 - T_u| ~ 0.09 near the fit, against a
+    # Monte Carlo noise of the cost of about 5e-3 at 2e5 packets
+    assert one.cost > 0.05
+    assert probed.refits == 0
+    assert list(probed.x) == list(one.x) and probed.cost == one.cost
+    assert probed.evals == one.evals + 4
