@@ -1,6 +1,6 @@
 // refcuda_bench.cu -- timing harness for the reference's own CUDA forward model.
 //
-// BASELINE infrastructure, not product code: it is compiled only by
+// Baseline infrastructure, not product code: it is compiled only by
 // oracle/build_ref.py:build_refcuda(), against an unmodified staged copy of the
 // reference's CUDA/CUDAISMLMC.h, and run only by bench.py's reference arm.
 //
