@@ -122,6 +122,11 @@ class ClockSampler:
                                          stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # nvidia-smi's start-up can hold up this process's CUDA calls for
+            # most of a second: time nothing before its first sample is in
+            t0 = time.perf_counter()
+            while not self.rows and self.proc.poll() is None and time.perf_counter() - t0 < 5.0:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
         return self
