@@ -21,15 +21,15 @@ integer tallies are summed into the merged result; a reduced-size sharded run
 is checked bit for bit against a single-process run of the same range.
 
 Reference arm (--impl reference): the reference's algorithm on the host cores,
-as restated in FP64 C from ISMLMC.py / MLMC.py (oracle/ismc_ref64.c: the
-reference itself is Python and cannot run on the GPU machine), each step a
-bounded packet sample of the same workload.
+as restated in FP64 C from ISMLMC.py / MLMC.py (oracle/ismc_ref64.c), each step
+a bounded packet sample of the same workload.
 Reference CUDA arm (--impl reference --workload refcuda): the reference's own
 CUDA kernel and host entry point (CUDA/CUDAISMLMC.h, compiled unmodified from a
 staged copy by oracle/build_ref.py) on the same GPU, in calls of 1e7 packets.
 Reference Python arm (--impl reference --workload refpython): the reference's
 own ISMLMC.py / MLMC.py (staged unmodified by oracle/build_ref.py) on every host
-core, one spawned process per core, each step a bounded packet sample.
+core, one spawned process per core, each step a bounded packet sample (or
+--packets per step when given).
 """
 import argparse
 import ctypes as C
@@ -402,36 +402,46 @@ def run_refpython(args, rank):
     procs = os.cpu_count()
     layers = refpython.layer_tuples(workload_layers(st))
     sph = refpython.sphere_dict(workload_spheres())
+    explicit = args.packets != PACKETS
     with refpython.Runner(model, procs) as pool:
-        # start the workers, then size one step to about 8 s of every core's
-        # time from the CPU seconds of a probe
+        # start the workers; without an explicit --packets, size one step to
+        # about 8 s of every core's time from the CPU seconds of a probe
         pool.run(layers, sph, 10, SEED)
         probe = 500
         for w in range(max(args.warmup, 1)):
             _, _, c = pool.run(layers, sph, probe, SEED + 1000 * (w + 1))
-        per_worker = max(probe, int(probe * 8.0 * procs / max(c, 1e-3)))
-        times, cpu, sums = [], 0.0, [0.0] * 5
+        if explicit:
+            per_worker = max(1, math.ceil(args.packets / procs))
+        else:
+            per_worker = max(probe, int(probe * 8.0 * procs / max(c, 1e-3)))
+        times, cpu, batches = [], 0.0, []
         for k in range(args.steps):
-            tallies, wall, c = pool.run(layers, sph, per_worker, SEED + 100000 * (k + 1))
+            _, wall, c = pool.run(layers, sph, per_worker, SEED + 100000 * (k + 1))
             times.append(wall)
             cpu += c
-            sums = [a + b for a, b in zip(sums, tallies)]
+            batches += pool.last_batches
     total = sum(times)
     per_step = per_worker * procs
     value = per_step * args.steps / total
+    # every worker's share is an independent batch of the reference's run
+    K = len(batches)
+    mean = [sum(b[i] for b in batches) / K for i in range(5)]
+    se = [math.sqrt(sum((b[i] - mean[i]) ** 2 for b in batches) / (K - 1) / K) if K > 1 else None
+          for i in range(5)]
     line = dict(base, value=value, n_gpus=1, steps=args.steps, warmup=args.warmup,
                 ms_per_step=1000 * total / args.steps, higher_is_better=True, scaling="weak",
                 vs_baseline=None, dtype="f64", data="synthetic",
                 config=dict(base["config"], packets_per_step=per_step,
-                            note="each step is a bounded packet sample of the workload"),
+                            note=("--packets per step, split over the processes" if explicit else
+                                  "each step is a bounded packet sample of the workload")),
                 cpu_baseline={"value": value, "unit": "photons/s", "cores": procs,
                               "kind": "reference",
                               "sample": f"{per_step} packets per step ({per_worker} on each of "
                                         f"{procs} processes), the reference's ISMLMC.py"},
                 e2e={"value": value, "unit": "photons/s", "h2d_bytes_per_step": 0,
                      "d2h_bytes_per_step": 0},
-                result={"tallies": ["A", "R_d", "R_s", "T_d", "T_u"],
-                        "mean": [v / args.steps for v in sums],
+                result={"tallies": ["A", "R_d", "R_s", "T_d", "T_u"], "mean": mean,
+                        "se": se, "batches": K,
                         "photons_per_cpu_second": per_step * args.steps / max(cpu, 1e-9)})
     print(json.dumps(line), flush=True)
 
@@ -753,7 +763,9 @@ def main():
     ap.add_argument("--stack", choices=["bench1", "bench1_noslides", "bench0", "bench0_noslides"],
                     default="bench1", help="layer stack of the forward workload (default: the "
                                            "multilayer benchmark configuration)")
-    ap.add_argument("--packets", type=int, default=PACKETS)
+    ap.add_argument("--packets", type=int, default=PACKETS,
+                    help="packets per step (the refpython arm sizes its steps itself unless "
+                         "this is given)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["forward", "lookup", "tables", "surrogate", "solve",
                                            "dropin", "train", "refcuda", "refpython"],

@@ -63,16 +63,19 @@ class Runner:
         self.model_dir = model_dir
         self.procs = procs
         self.pool = mp.get_context("spawn").Pool(procs)
+        self.last_batches = []
 
     def run(self, layers, sph, packets_per_worker, seed):
         """All workers simulate `packets_per_worker` packets each (worker k
         seeded with seed + k).  Returns (pooled tallies, wall seconds, CPU
-        seconds summed over workers)."""
+        seconds summed over workers).  The workers' own tallies are kept in
+        self.last_batches."""
         jobs = [(self.model_dir, layers, sph, int(packets_per_worker), seed + k)
                 for k in range(self.procs)]
         t0 = time.perf_counter()
         res = self.pool.map(_batch, jobs)
         wall = time.perf_counter() - t0
+        self.last_batches = [r[0] for r in res]
         tallies = [sum(r[0][i] for r in res) / len(res) for i in range(5)]
         return tallies, wall, sum(r[1] for r in res)
 
