@@ -216,11 +216,34 @@ def cpu_solve_baseline(engine, seconds=60.0, packets=100_000):
         errs.append([abs(res.x[0] / truth[k, 0] - 1), abs(res.x[1] / truth[k, 1] - 1)])
         done += 1
     dt = time.perf_counter() - t0
-    return {"value": done / dt, "unit": "solves/s", "cores": threads, "kind": "port",
-            "sample": f"{done} solves of the benchmark's measurements, scipy Powell (tol 1e-3, at most "
-                      f"400 evaluations) on the reference's cost with {packets}-packet FP64 C "
-                      f"restatement runs ({threads} threads), {evals[0]} evaluations, {dt:.1f} s",
-            "rel_err_vs_truth_median": np.median(np.array(errs), 0).tolist()}
+    out = {"value": done / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+           "sample": f"{done} solves of the benchmark's measurements, scipy Powell (tol 1e-3, at most "
+                     f"400 evaluations) on the reference's cost with {packets}-packet FP64 C "
+                     f"restatement runs ({threads} threads), {evals[0]} evaluations, {dt:.1f} s",
+           "rel_err_vs_truth_median": np.median(np.array(errs), 0).tolist()}
+    # The same objective on the reference's own Python forward model: one
+    # N-packet ISMLMC() run at each solved measurement's truth, spread over
+    # every core, scaled by the evaluations per solve that Powell took above
+    from oracle import build_ref, refpython
+    model = build_ref.staged_python()
+    if model and done:
+        S = refpython.sphere_dict(sph)
+        per = math.ceil(packets / threads)
+        walls = []
+        with refpython.Runner(model, threads) as pool:
+            pool.run(refpython.layer_tuples(sample_stack(1.0, 10.0, 0.9, 0.1, 1.4)), S, 10, 1)
+            for k in range(done):
+                L = refpython.layer_tuples(sample_stack(truth[k, 0], truth[k, 1], 0.9, 0.1, 1.4))
+                walls.append(pool.run(L, S, per, 100 + k)[1])
+        t_obj = sum(walls) / len(walls)
+        eps = evals[0] / done
+        out["reference_python"] = {
+            "objective_s": t_obj, "evals_per_solve": eps,
+            "solves_per_s_extrapolated": 1.0 / (eps * t_obj),
+            "sample": f"{per * threads}-packet runs of the reference's ISMLMC.py at {done} truths "
+                      f"({threads} processes), mean {t_obj:.2f} s per objective, times the "
+                      f"{eps:.0f} Powell evaluations per solve measured on the restatement"}
+    return out
 
 
 def cpu_tables_baseline(data, N=1000, M=100, cells_sample=300, seed=3):
