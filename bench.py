@@ -280,7 +280,7 @@ def cpu_tables_baseline(data, N=1000, M=100, cells_sample=300, seed=3):
             "griddata_s": t_grid, "uncertainty_s_scaled": per_cell * len(ok)}
 
 
-def cpu_lookup_baseline(r, seconds=20.0, sample=64):
+def cpu_lookup_baseline(r, seconds=20.0, sample=64, ref_seconds=30.0):
     """The FP64 restatement of the reference on a stratified sample of the
     lookup workload's instances (every k-th of the 4608, budgets capped so the
     sample takes about `seconds`), on all host cores; the full workload's CPU
@@ -309,11 +309,43 @@ def cpu_lookup_baseline(r, seconds=20.0, sample=64):
         steps += st
     dt = time.perf_counter() - t0
     sps = steps / dt
-    return {"value": packets / dt, "unit": "photons/s", "cores": threads, "kind": "port",
-            "steps_per_s": sps,
-            "sample": f"{len(pick)} instances (every {stride}th of the workload), at most {cap} packets "
-                      f"each, FP64 C restatement on {threads} threads, {dt:.1f} s",
-            "full_workload_s_extrapolated": r["steps_per_s"] * r["seconds"] / sps}
+    out = {"value": packets / dt, "unit": "photons/s", "cores": threads, "kind": "port",
+           "steps_per_s": sps,
+           "sample": f"{len(pick)} instances (every {stride}th of the workload), at most {cap} packets "
+                     f"each, FP64 C restatement on {threads} threads, {dt:.1f} s",
+           "full_workload_s_extrapolated": r["steps_per_s"] * r["seconds"] / sps}
+    # The reference's own Python on the same instances; the restatement runs
+    # the very same instances and packet counts again, and the ratio of the
+    # two times scales the extrapolated full-workload time
+    from oracle import build_ref, refpython
+    model = build_ref.staged_python()
+    if model:
+        args = [refpython.instance_args(x) for x in pick]
+        with refpython.Runner(model, threads) as pool:
+            pool.run(*args[0], 1, 1)
+            probe = 200
+            t0 = time.perf_counter()
+            for a in args[:8]:
+                pool.run(*a, probe, 3)
+            per = (time.perf_counter() - t0) / 8 / probe     # s per packet of one process
+            each = max(probe, int(ref_seconds / max(per * len(args), 1e-9)))
+            t0 = time.perf_counter()
+            for k, a in enumerate(args):
+                pool.run(*a, each, 100 + k)
+            dt_r = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for x in pick:
+            x.n_packets = each * threads
+            oracle.ref64_run(x, threads=threads)
+        dt_p = time.perf_counter() - t0
+        out["reference_python"] = {
+            "value": each * threads * len(args) / dt_r, "unit": "photons/s",
+            "sample": f"the same {len(args)} instances at {each * threads} packets each, the "
+                      f"reference's ISMLMC.py in {threads} processes, {dt_r:.1f} s; the "
+                      f"restatement on the same packets {dt_p:.2f} s",
+            "time_vs_restatement": dt_r / dt_p,
+            "full_workload_s_extrapolated": out["full_workload_s_extrapolated"] * dt_r / dt_p}
+    return out
 
 
 def run_dropin_workload(calls=200, N=10_000):

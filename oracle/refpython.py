@@ -56,6 +56,18 @@ def sphere_dict(sp):
     return {k: getattr(sp, k) for k in keys}
 
 
+def instance_args(inst):
+    """(layer tuples, sphere arguments) of an ismc_gb300 ctypes instance."""
+    st, sp = inst.stack, inst.spheres
+    layers = [(float(st.n[l]), float(st.mua[l]), float(st.mus[l]), float(st.g[l]), float(st.d[l]))
+              for l in range(int(st.L))]
+    keys = ("R_pw", "R_fs", "R_fp", "R_fd", "R_f", "R_angle",
+            "T_pw", "T_fs", "T_fp", "T_fd", "T_f", "T_angle")
+    sph = {k: float(getattr(sp, k)) for k in keys}
+    sph.update(R=bool(sp.R), T=bool(sp.T), specular_included=bool(sp.specular_included))
+    return layers, sph
+
+
 class Runner:
     """A pool of `procs` spawned workers running the staged reference model."""
 
