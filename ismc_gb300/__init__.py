@@ -9,9 +9,9 @@ include/ismc.h); build it with ``python -m ismc_gb300.build``.
 """
 from .api import (Engine, IsmcError, Layer, Result, Spheres, cap_fraction, default_engine,
                   instance_array, load_library, make_instance, make_solve, make_stack, make_spheres, make_tune,
-                  tally_to_result)
+                  merge_tallies, split_instance, tally_to_result)
 from . import _abi
 
 __all__ = ["Engine", "IsmcError", "Layer", "Result", "Spheres", "cap_fraction", "default_engine",
            "instance_array", "load_library", "make_instance", "make_solve", "make_stack", "make_spheres",
-           "make_tune", "tally_to_result", "_abi"]
+           "make_tune", "merge_tallies", "split_instance", "tally_to_result", "_abi"]

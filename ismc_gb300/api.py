@@ -200,11 +200,22 @@ class Result:
 def tally_to_result(t: _abi.Tally) -> Result:
     """FP64 normalisation of the fixed-point sums: mean = S/(N 2^k),
     SE = sqrt((Q/(N 2^k) - mean^2) / (N - 1))."""
-    n = int(t.n)
-    scale = float(2 ** int(t.scale_log2 or 32))
+    return merge_tallies([t])
+
+
+def merge_tallies(tallies) -> Result:
+    """One Result from the tallies of consecutive packet ranges of one
+    simulation (split_instance): the integer sums add exactly (Python
+    integers, so beyond 64 bits too), statuses combine by minimum (any error
+    wins), and the normalisation is tally_to_result's."""
+    t0 = tallies[0]
+    n = sum(int(t.n) for t in tallies)
+    sums = [sum(int(t.sum[k]) for t in tallies) for k in range(5)]
+    sumsqs = [sum(int(t.sumsq[k]) for t in tallies) for k in range(5)]
+    scale = float(2 ** int(t0.scale_log2 or 32))
     mean, se = [], []
     for k in range(5):
-        s, q = int(t.sum[k]), int(t.sumsq[k])
+        s, q = sums[k], sumsqs[k]
         if n > 0:
             m = s / scale / n
             ex2 = q / scale / n
@@ -214,12 +225,28 @@ def tally_to_result(t: _abi.Tally) -> Result:
         else:
             mean.append(float("nan"))
             se.append(float("nan"))
-    return Result(n=n, mean=mean, se=se, status=int(t.status), steps=int(t.steps),
-                  events=int(t.events), reincidences=int(t.reincidences), capped=int(t.capped),
-                  trapped=int(t.trapped),
-                  analytic_specular=float(t.analytic_specular),
-                  analytic_ballistic=float(t.analytic_ballistic),
-                  sums=[int(x) for x in t.sum], sumsqs=[int(x) for x in t.sumsq])
+    total = lambda f: sum(int(getattr(t, f)) for t in tallies)
+    return Result(n=n, mean=mean, se=se, status=min(int(t.status) for t in tallies),
+                  steps=total("steps"), events=total("events"),
+                  reincidences=total("reincidences"), capped=total("capped"),
+                  trapped=total("trapped"), analytic_specular=float(t0.analytic_specular),
+                  analytic_ballistic=float(t0.analytic_ballistic), sums=sums, sumsqs=sumsqs)
+
+
+def split_instance(inst: _abi.Instance, max_packets: int = _abi.MAX_PACKETS):
+    """An instance as consecutive packet ranges of at most max_packets each.
+    Every draw is keyed by the packet id, so the parts' summed tallies equal
+    one run of the whole range (ISMC_MAX_PACKETS bounds one instance)."""
+    n = int(inst.n_packets)
+    if n <= max_packets:
+        return [inst]
+    parts = []
+    for lo in range(0, n, max_packets):
+        x = _abi.Instance.from_buffer_copy(bytes(inst))
+        x.packet_offset = int(inst.packet_offset) + lo
+        x.n_packets = min(max_packets, n - lo)
+        parts.append(x)
+    return parts
 
 
 def tallies_mean_se(tallies):
@@ -369,6 +396,10 @@ class Engine:
     # -- single instance: ismc_run (MLMC.py roulette 1e-4 / m 10)
     def run(self, layers: Sequence[Layer], spheres: Spheres, n_packets: int, seed: int = 0,
             mode="compat") -> Result:
+        if int(n_packets) > _abi.MAX_PACKETS:
+            # the instance ismc_run builds, in parts of at most ISMC_MAX_PACKETS
+            return self.run_batch([make_instance(layers, spheres, n_packets, seed=seed,
+                                                 mode=mode)])[0]
         st = make_stack(layers)
         sp = make_spheres(spheres)
         out = _abi.Tally()
@@ -387,8 +418,23 @@ class Engine:
         self._check(rc)
         return out
 
-    def run_batch(self, instances, tune: Optional[_abi.Tune] = None) -> List[Result]:
-        return [tally_to_result(t) for t in self.run_batch_raw(instances, tune)]
+    def run_batch(self, instances, tune: Optional[_abi.Tune] = None,
+                  max_packets: int = _abi.MAX_PACKETS) -> List[Result]:
+        """Results of a batch in one launch.  An instance of more than
+        max_packets packets (at most ISMC_MAX_PACKETS, the C ABI's limit) runs
+        as consecutive packet ranges in the same launch, merged exactly."""
+        insts = list(instances)
+        if all(int(x.n_packets) <= max_packets for x in insts):
+            return [tally_to_result(t) for t in self.run_batch_raw(instances, tune)]
+        parts, owner = [], []
+        for i, x in enumerate(insts):
+            for p in split_instance(x, max_packets):
+                parts.append(p)
+                owner.append(i)
+        groups = [[] for _ in insts]
+        for t, i in zip(self.run_batch_raw(parts, tune), owner):
+            groups[i].append(t)
+        return [merge_tallies(g) for g in groups]
 
     def run_batch_device(self, d_inst_ptr: int, n_inst: int, d_out_ptr: int, stream_ptr: int = 0,
                          tune: Optional[_abi.Tune] = None):

@@ -103,3 +103,19 @@ def test_packet_count_beyond_tally_headroom(engine):
     assert out[1].status == _abi.ERR_CAPACITY and out[1].n == 0 and list(out[1].sum) == [0] * 5
     # the context stays usable
     assert engine.run_batch_raw([good])[0].status == 0
+
+
+def test_instance_above_the_packet_limit_runs_in_parts(engine):
+    """Engine.run_batch runs an instance of more than max_packets packets
+    (ISMC_MAX_PACKETS by default) as consecutive packet ranges in the same
+    launch.  Every draw is keyed by the packet id, so the merged tallies equal
+    one run of the whole range bit for bit."""
+    from ismc_gb300.workloads import bench1_layers
+    inst = make_instance(bench1_layers(), bench_spheres(), 3_500_000, seed=12, packet_offset=5)
+    whole = engine.run_batch([inst])[0]
+    parts = engine.run_batch([inst], max_packets=1_000_000)[0]
+    assert parts.status == 0
+    assert parts.sums == whole.sums and parts.sumsqs == whole.sumsqs
+    assert (parts.n, parts.steps, parts.events, parts.reincidences, parts.trapped) == \
+        (whole.n, whole.steps, whole.events, whole.reincidences, whole.trapped)
+    assert parts.mean == whole.mean and parts.se == whole.se

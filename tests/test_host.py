@@ -3,6 +3,7 @@ tally normalisation agree with their one-at-a-time counterparts."""
 import math
 
 import numpy as np
+import pytest
 
 from ismc_gb300 import _abi, api
 from ismc_gb300.surrogate import sample_stack
@@ -119,3 +120,43 @@ def test_reference_cuda_arm_refuses_stacks_with_slides(capsys):
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["workload"] == "refcuda"
     assert "slides" in line["unavailable"]
+
+
+def test_split_instance_covers_the_packet_range_once():
+    """An instance above the per-instance packet limit becomes consecutive
+    packet ranges of the same simulation."""
+    from ismc_gb300 import Layer, Spheres, make_instance, split_instance
+    inst = make_instance([Layer(1.4, 1.0, 100.0, 0.9, 0.1)], Spheres(), 10_500_000, seed=3,
+                         packet_offset=7)
+    assert split_instance(inst) == [inst]
+    parts = split_instance(inst, max_packets=4_000_000)
+    assert [(int(p.packet_offset), int(p.n_packets)) for p in parts] == \
+        [(7, 4_000_000), (4_000_007, 4_000_000), (8_000_007, 2_500_000)]
+    for p in parts:
+        assert bytes(p.stack) == bytes(inst.stack) and int(p.seed) == 3
+
+
+def test_merge_tallies_adds_exactly_beyond_64_bits():
+    """Merged tallies keep exact integer sums (past 2^64) and normalise like a
+    single tally."""
+    from ismc_gb300 import _abi, merge_tallies, tally_to_result
+    a, b = _abi.Tally(), _abi.Tally()
+    for t, n, w in ((a, 1000, 0.25), (b, 3000, 0.75)):
+        t.n = n
+        t.scale_log2 = 32
+        t.sum[1] = int(n * w * 2 ** 32)
+        t.sumsq[1] = int(n * w * w * 2 ** 32)
+        t.steps = n * 10
+    m = merge_tallies([a, b])
+    assert m.n == 4000 and m.steps == 40000
+    assert m.mean[1] == pytest.approx((250 + 2250) / 4000, rel=1e-15)
+    one = tally_to_result(a)
+    assert one.mean[1] == pytest.approx(0.25, rel=1e-15) and one.se[1] == 0.0
+    big = [_abi.Tally() for _ in range(3)]
+    for t in big:
+        t.n = 2 ** 31
+        t.scale_log2 = 32
+        t.sum[0] = 2 ** 63                      # weight 1 per packet at 2^32
+        t.sumsq[0] = 2 ** 63
+    r = merge_tallies(big)
+    assert r.sums[0] == 3 * 2 ** 63 and r.mean[0] == 1.0 and r.se[0] == 0.0
