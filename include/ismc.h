@@ -103,8 +103,9 @@ typedef struct ismc_spheres {
  * the 2^64 range of any sum or sum of squares.  A larger simulation is split
  * into instances with consecutive packet_offset ranges; their tallies add
  * exactly, in wider than 64-bit arithmetic once the total passes 2^31
- * packets.  Instances beyond the limit are refused with ISMC_ERR_CAPACITY
- * instead of returning wrapped sums.
+ * packets (the Python API's Engine.run_batch does this split and sum).
+ * Instances beyond the limit are refused with ISMC_ERR_CAPACITY instead of
+ * returning wrapped sums.
  */
 #define ISMC_MAX_PACKETS 2147483648ull
 
