@@ -20,9 +20,12 @@ stack (weak scaling), the max time over ranks is reported, and the ranks'
 integer tallies are summed into the merged result; a reduced-size sharded run
 is checked bit for bit against a single-process run of the same range.
 
-Reference arm (--impl reference): the reference's algorithm on the host cores,
-as restated in FP64 C from ISMLMC.py / MLMC.py (oracle/ismc_ref64.c), each step
-a bounded packet sample of the same workload.
+Reference arm (--impl reference): the reference's own ISMLMC.py / MLMC.py on
+every host core where oracle/build_ref.py staged them (as --workload refpython,
+below), else the reference's algorithm as restated in FP64 C
+(oracle/ismc_ref64.c); each step a bounded packet sample of the same workload.
+The GPU arm's cpu_baseline is the same reference Python (with the restatement
+beside it), or the restatement alone.
 Reference CUDA arm (--impl reference --workload refcuda): the reference's own
 CUDA kernel and host entry point (CUDA/CUDAISMLMC.h, compiled unmodified from a
 staged copy by oracle/build_ref.py) on the same GPU, in calls of 1e7 packets.
@@ -401,7 +404,15 @@ def load_roofline_profile():
 
 # ----------------------------------------------------------------------------
 def run_reference(args, rank, world):
+    """The reference arm: the reference's own ISMLMC.py where
+    oracle/build_ref.py staged it (steps sized so the whole run takes about
+    2.5 minutes), else the FP64 C restatement (oracle/ismc_ref64.c)."""
     if rank != 0:
+        return
+    from oracle import build_ref
+    if build_ref.staged_python():
+        run_refpython(args, rank,
+                      step_seconds=min(8.0, max(2.0, 150.0 / (args.steps + max(args.warmup, 1)))))
         return
     import oracle
     oracle.lib()
@@ -438,16 +449,43 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def run_refpython(args, rank):
+def refpython_baseline(seconds=12.0, stack="bench1"):
+    """The reference's own ISMLMC.py (staged by oracle/build_ref.py) on every
+    host core, on a bounded packet sample of the workload (about `seconds` of
+    every core's time); None where it was not staged."""
+    from oracle import build_ref, refpython
+    model = build_ref.staged_python()
+    if not model:
+        return None
+    procs = os.cpu_count()
+    layers = refpython.layer_tuples(workload_layers(stack))
+    sph = refpython.sphere_dict(workload_spheres())
+    with refpython.Runner(model, procs) as pool:
+        pool.run(layers, sph, 10, SEED)
+        probe = 500
+        _, _, c = pool.run(layers, sph, probe, SEED + 1000)
+        per_worker = max(probe, int(probe * seconds * procs / max(c, 1e-3)))
+        _, wall, _ = pool.run(layers, sph, per_worker, SEED + 100000)
+    n = per_worker * procs
+    return {"value": n / wall, "unit": "photons/s", "cores": procs, "kind": "reference",
+            "sample": f"{n} packets of the workload ({per_worker} on each of {procs} processes), "
+                      f"the reference's ISMLMC.py, {wall:.1f} s"}
+
+
+def run_refpython(args, rank, step_seconds=8.0):
     """The reference's own Python forward model on every host core (--impl
-    reference --workload refpython): ISMLMC() of the unmodified ISMLMC.py /
-    MLMC.py that oracle/build_ref.py stages, one spawned process per core, each
-    step a bounded packet sample of the chosen stack (oracle/refpython.py)."""
+    reference --workload refpython, and the reference arm itself where the
+    model was staged): ISMLMC() of the unmodified ISMLMC.py / MLMC.py that
+    oracle/build_ref.py stages, one spawned process per core, each step a
+    bounded packet sample of the chosen stack (about step_seconds of every
+    core's time) unless --packets is given (oracle/refpython.py)."""
     if rank != 0:
         return
     st = args.stack
-    base = {"impl": "reference", "workload": "refpython", "metric": "photons/s",
-            "unit": "photons/s", "config": workload_config(st, args.packets)}
+    base = {"impl": "reference", "metric": "photons/s", "unit": "photons/s",
+            "config": workload_config(st, args.packets)}
+    if args.workload == "refpython":
+        base["workload"] = "refpython"
     from oracle import build_ref, refpython
     model = build_ref.staged_python()
     if not model:
@@ -468,7 +506,7 @@ def run_refpython(args, rank):
         if explicit:
             per_worker = max(1, math.ceil(args.packets / procs))
         else:
-            per_worker = max(probe, int(probe * 8.0 * procs / max(c, 1e-3)))
+            per_worker = max(probe, int(probe * step_seconds * procs / max(c, 1e-3)))
         times, cpu, batches = [], 0.0, []
         for k in range(args.steps):
             _, wall, c = pool.run(layers, sph, per_worker, SEED + 100000 * (k + 1))
@@ -483,7 +521,8 @@ def run_refpython(args, rank):
     mean = [sum(b[i] for b in batches) / K for i in range(5)]
     se = [math.sqrt(sum((b[i] - mean[i]) ** 2 for b in batches) / (K - 1) / K) if K > 1 else None
           for i in range(5)]
-    line = dict(base, value=value, n_gpus=1, steps=args.steps, warmup=args.warmup,
+    line = dict(base, value=value, n_gpus=int(os.environ.get("WORLD_SIZE", "1")),
+                steps=args.steps, warmup=args.warmup,
                 ms_per_step=1000 * total / args.steps, higher_is_better=True, scaling="weak",
                 vs_baseline=None, dtype="f64", data="synthetic",
                 config=dict(base["config"], packets_per_step=per_step,
@@ -706,7 +745,16 @@ def run_gpu(args, rank, world, dist):
         gbs = prof["dram_bytes_per_launch"] / (dev_time / args.steps) / 1e9
         roof["hbm"] = {"achieved_gbs": gbs, "peak_gbs": peaks["hbm_gbs"],
                        "frac": gbs / peaks["hbm_gbs"], "peak_source": "MEASURED_PEAKS.json (of measured)"}
-    cpu = cpu_baseline(stack=st) if (world == 1 and not args.no_cpu_baseline) else None
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        # the reference's own Python where it was staged, with the FP64
+        # restatement beside it; else the restatement
+        port = cpu_baseline(stack=st)
+        cpu = refpython_baseline(stack=st)
+        if cpu is None:
+            cpu = port
+        else:
+            cpu["port"] = port
     line = {"metric": "photons/s", "value": value, "unit": "photons/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dev_time / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",

@@ -77,3 +77,25 @@ def test_shard_range_covers_exactly():
             assert sum(c for _, c in ranges) == n
             for (a, c), (b, _) in zip(ranges, ranges[1:]):
                 assert a + c == b
+
+
+def test_bench_reference_arm_under_torchrun_two_ranks():
+    """`bench.py --impl reference` launched as the multi-GPU runs launch it
+    (torchrun, two ranks, gloo on CPU): rank 0 alone runs the reference and
+    prints one JSON line; the other rank exits 0 without work."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()),
+           os.path.join(root, "bench.py"), "--impl", "reference", "--gpus", "2", "--steps", "1",
+           "--warmup", "1", "--packets", "2000"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=900, cwd=root)
+    assert r.returncode == 0, r.stderr[-3000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout[-2000:]
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
