@@ -105,6 +105,14 @@ def workload_config(stack="bench1", packets=PACKETS):
 CONFIG = workload_config()
 
 
+def host_cores():
+    """Host cores this process may run on (its CPU affinity), for the CPU arms."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
 # ----------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
@@ -165,7 +173,7 @@ def cpu_baseline(seconds=12.0, stack="bench1"):
     """The reference's algorithm (FP64 restatement of ISMLMC.py) on all host
     cores, on a bounded packet sample of the workload."""
     import oracle
-    threads = os.cpu_count()
+    threads = host_cores()
     n = 20000
     t0 = time.perf_counter()
     oracle.ref64_run(workload_instance(n, stack=stack), threads=threads)
@@ -193,7 +201,7 @@ def cpu_solve_baseline(engine, seconds=60.0, packets=100_000):
     from ismc_gb300.benchmarks import make_measurements
     from ismc_gb300.surrogate import sample_stack
     from ismc_gb300.workloads import bench_spheres
-    threads = os.cpu_count()
+    threads = host_cores()
     sph = bench_spheres()
     truth, meas = make_measurements(engine, 8, seed=4)
     evals = [0]
@@ -294,7 +302,7 @@ def cpu_lookup_baseline(r, seconds=20.0, sample=64, ref_seconds=30.0):
     insts = lookup_grid(seed=2, scale=r.get("scale", 1.0))
     stride = max(1, len(insts) // sample)
     pick = [copy.copy(insts[i]) for i in range(0, len(insts), stride)][:sample]
-    threads = os.cpu_count()
+    threads = host_cores()
     cap = 2000
     t0 = time.perf_counter()
     for x in pick[:8]:
@@ -416,7 +424,7 @@ def run_reference(args, rank, world):
         return
     import oracle
     oracle.lib()
-    threads = os.cpu_count()
+    threads = host_cores()
     # size one step to ~10 s of host work
     n = 20000
     st = args.stack
@@ -457,7 +465,7 @@ def refpython_baseline(seconds=12.0, stack="bench1"):
     model = build_ref.staged_python()
     if not model:
         return None
-    procs = os.cpu_count()
+    procs = host_cores()
     layers = refpython.layer_tuples(workload_layers(stack))
     sph = refpython.sphere_dict(workload_spheres())
     with refpython.Runner(model, procs) as pool:
@@ -492,7 +500,7 @@ def run_refpython(args, rank, step_seconds=8.0):
         print(json.dumps(dict(base, unavailable="the reference's Python model was not staged into "
                               "oracle/_ref/python (oracle/build_ref.py stage())")), flush=True)
         return
-    procs = os.cpu_count()
+    procs = host_cores()
     layers = refpython.layer_tuples(workload_layers(st))
     sph = refpython.sphere_dict(workload_spheres())
     explicit = args.packets != PACKETS
