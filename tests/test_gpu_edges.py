@@ -38,6 +38,18 @@ def test_sixteen_layer_stack(engine, mode):
     assert g.steps > 0
 
 
+@pytest.mark.parametrize("mode", ["compat", "physical"])
+def test_anisotropy_extremes_and_index_matched_layers(engine, mode):
+    """Back-scattering (g = -0.9), strongly forward (g = 0.99) and undeflected
+    (g = 1) layers, an isotropic one (g = 0), and tissue index-matched to the
+    ambient (n = 1, Fresnel reflectance 0 at normal incidence), with both
+    spheres."""
+    layers = [Layer(1.0, 0.5, 40.0, -0.9, 0.1), Layer(1.0, 0.2, 60.0, 0.99, 0.1),
+              Layer(1.33, 0.3, 30.0, 1.0, 0.05), Layer(1.33, 0.1, 20.0, 0.0, 0.05)]
+    g = _check(engine, make_instance(layers, bench_spheres(), 20000, seed=21, mode=mode))
+    assert g.steps > 0
+
+
 def test_packet_ids_above_2_pow_32(engine):
     """Packet ids feed two counter words of Philox: ranges crossing 2^32 and far
     above it are drawn exactly as the twin draws them."""
