@@ -58,3 +58,26 @@ def bench1_layers():
     return [Layer.slide(1.52, 0.1), Layer(1.37, 0.5, 200.0, 0.8, 0.01),
             Layer(1.40, 2.0, 120.0, 0.9, 0.15), Layer(1.44, 0.2, 50.0, 0.75, 0.3),
             Layer.slide(1.52, 0.1)]
+
+
+# Stacks outside the golden runs' range, checked against the FP64
+# restatement of the reference's walk (oracle/ismc_ref64.c):
+#   anisotropy_extremes  g = -0.9, 0.99, 1 and 0; two layers index-matched to
+#                        the ambient (n = 1); the benchmark spheres
+#   index_contrast       n = 2.4 tissue 20 um thick under an n = 1.8 slide, a
+#                        strong absorber (mua 30), a highly scattering layer
+#                        (mus 300, g 0.95), an n = 1.45 slide; large ports,
+#                        unequal walls and both angle thresholds
+def extreme_stacks():
+    return {
+        "anisotropy_extremes": (
+            [Layer(1.0, 0.5, 40.0, -0.9, 0.1), Layer(1.0, 0.2, 60.0, 0.99, 0.1),
+             Layer(1.33, 0.3, 30.0, 1.0, 0.05), Layer(1.33, 0.1, 20.0, 0.0, 0.05)],
+            bench_spheres()),
+        "index_contrast": (
+            [Layer.slide(1.8, 0.05), Layer(2.4, 0.2, 80.0, 0.85, 0.002),
+             Layer(1.33, 30.0, 5.0, 0.5, 0.05), Layer(1.55, 0.05, 300.0, 0.95, 0.08),
+             Layer.slide(1.45, 0.2)],
+            Spheres(R=True, R_pw=0.995, R_fs=0.08, R_fp=0.06, R_fd=0.02, R_angle=0.3,
+                    T=True, T_pw=0.9, T_fs=0.12, T_fp=0.01, T_fd=0.05, T_angle=0.01)),
+    }

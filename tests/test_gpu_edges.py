@@ -6,6 +6,7 @@ import ctypes as C
 
 import pytest
 
+import cases
 import oracle
 from ismc_gb300 import Layer, Spheres, _abi, make_instance
 from ismc_gb300.workloads import bench_spheres
@@ -39,14 +40,13 @@ def test_sixteen_layer_stack(engine, mode):
 
 
 @pytest.mark.parametrize("mode", ["compat", "physical"])
-def test_anisotropy_extremes_and_index_matched_layers(engine, mode):
-    """Back-scattering (g = -0.9), strongly forward (g = 0.99) and undeflected
-    (g = 1) layers, an isotropic one (g = 0), and tissue index-matched to the
-    ambient (n = 1, Fresnel reflectance 0 at normal incidence), with both
-    spheres."""
-    layers = [Layer(1.0, 0.5, 40.0, -0.9, 0.1), Layer(1.0, 0.2, 60.0, 0.99, 0.1),
-              Layer(1.33, 0.3, 30.0, 1.0, 0.05), Layer(1.33, 0.1, 20.0, 0.0, 0.05)]
-    g = _check(engine, make_instance(layers, bench_spheres(), 20000, seed=21, mode=mode))
+@pytest.mark.parametrize("name", sorted(cases.extreme_stacks()))
+def test_extreme_stacks(engine, name, mode):
+    """Anisotropy extremes (g = -0.9, 0.99, 1, 0) with index-matched layers,
+    and strong index contrast with a 20 um layer, a strong absorber and
+    large ports (tests/cases.py extreme_stacks)."""
+    layers, sph = cases.extreme_stacks()[name]
+    g = _check(engine, make_instance(layers, sph, 20000, seed=21, mode=mode))
     assert g.steps > 0
 
 

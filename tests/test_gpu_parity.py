@@ -155,17 +155,18 @@ def test_gpu_ballistic_mc_matches_analytic(engine):
     assert r["R_d"] == 0.0 and r["T_d"] == 0.0
 
 
-def test_gpu_anisotropy_extremes_match_fp64_restatement(engine):
-    """Back-scattering (g = -0.9), strongly forward (g = 0.99), undeflected
-    (g = 1) and isotropic layers, two of them index-matched to the ambient
-    (n = 1), both spheres: the GPU (2e6 packets) against the FP64 restatement
-    of the reference's walk (oracle/ismc_ref64.c, 4e5 packets) within 3
-    combined standard errors per tally.  The golden runs of the reference
-    cover g in [0.6, 0.95] and 0 only."""
-    layers = [Layer(1.0, 0.5, 40.0, -0.9, 0.1), Layer(1.0, 0.2, 60.0, 0.99, 0.1),
-              Layer(1.33, 0.3, 30.0, 1.0, 0.05), Layer(1.33, 0.1, 20.0, 0.0, 0.05)]
-    r = engine.run_batch([make_instance(layers, cases.bench_spheres(), 2_000_000, seed=22)])[0]
-    m, se, _ = oracle.ref64_run(make_instance(layers, cases.bench_spheres(), 400_000, seed=23))
+@pytest.mark.parametrize("name", sorted(cases.extreme_stacks()))
+def test_gpu_extreme_stacks_match_fp64_restatement(engine, name):
+    """Stacks the golden runs do not reach (tests/cases.py extreme_stacks:
+    anisotropy extremes and index-matched layers; strong index contrast,
+    a 20 um layer, a strong absorber, large ports): the GPU at 2e6 packets
+    against the FP64 restatement of the reference's walk
+    (oracle/ismc_ref64.c) at 4e5 packets, within 3 combined standard errors
+    per tally.  The GPU's tallies are the twin's bit for bit
+    (test_gpu_edges.py), whose CPU test makes the same comparison."""
+    layers, sph = cases.extreme_stacks()[name]
+    r = engine.run_batch([make_instance(layers, sph, 2_000_000, seed=22)])[0]
+    m, se, _ = oracle.ref64_run(make_instance(layers, sph, 400_000, seed=23))
     z = cases.zscores(r.mean, r.se, m, se)
     assert r.status == 0 and max(abs(x) for x in z) <= 3.0, (z, r.mean, m)
 

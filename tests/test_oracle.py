@@ -58,18 +58,17 @@ def test_twin_vs_ref64_large_n():
     assert max(abs(x) for x in z) <= Z_FAMILY, z
 
 
-def test_twin_vs_ref64_anisotropy_extremes():
-    """The FP32 twin's division-free Henyey-Greenstein and rotation algebra
-    against the FP64 restatement of the reference's walk where the golden
-    runs do not reach: g = -0.9, 0.99, 1 and 0, two layers index-matched to
-    the ambient (n = 1), both spheres; 3 combined standard errors per tally
-    (the GPU test of the same stack draws the same twin-exact tallies)."""
-    from ismc_gb300 import Layer, make_instance
-    layers = [Layer(1.0, 0.5, 40.0, -0.9, 0.1), Layer(1.0, 0.2, 60.0, 0.99, 0.1),
-              Layer(1.33, 0.3, 30.0, 1.0, 0.05), Layer(1.33, 0.1, 20.0, 0.0, 0.05)]
-    r = tally_to_result(oracle.twin_run(make_instance(layers, cases.bench_spheres(), 2_000_000,
-                                                      seed=22)))
-    mean, se, _ = oracle.ref64_run(make_instance(layers, cases.bench_spheres(), 400_000, seed=23))
+@pytest.mark.parametrize("name", sorted(cases.extreme_stacks()))
+def test_twin_vs_ref64_extreme_stacks(name):
+    """The FP32 twin's division-free Henyey-Greenstein, rotation and Fresnel
+    algebra against the FP64 restatement of the reference's walk on stacks
+    the golden runs do not reach (tests/cases.py extreme_stacks), 3 combined
+    standard errors per tally.  The GPU draws the twin's tallies bit for
+    bit, so its test of the same stacks sees the same z-scores."""
+    layers, sph = cases.extreme_stacks()[name]
+    from ismc_gb300 import make_instance
+    r = tally_to_result(oracle.twin_run(make_instance(layers, sph, 2_000_000, seed=22)))
+    mean, se, _ = oracle.ref64_run(make_instance(layers, sph, 400_000, seed=23))
     z = cases.zscores(r.mean, r.se, mean, se)
     assert max(abs(x) for x in z) <= 3.0, z
 
