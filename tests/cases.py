@@ -68,6 +68,10 @@ def bench1_layers():
 #                        strong absorber (mua 30), a highly scattering layer
 #                        (mus 300, g 0.95), an n = 1.45 slide; large ports,
 #                        unequal walls and both angle thresholds
+#   sphere_extremes      a thin slab between slides under a lossless R sphere
+#                        (wall 1.0) with a 0.2 % sample port and a 30 %
+#                        entrance port; no T sphere, with a zero acceptance
+#                        angle
 def extreme_stacks():
     return {
         "anisotropy_extremes": (
@@ -80,4 +84,8 @@ def extreme_stacks():
              Layer.slide(1.45, 0.2)],
             Spheres(R=True, R_pw=0.995, R_fs=0.08, R_fp=0.06, R_fd=0.02, R_angle=0.3,
                     T=True, T_pw=0.9, T_fs=0.12, T_fp=0.01, T_fd=0.05, T_angle=0.01)),
+        "sphere_extremes": (
+            [Layer.slide(1.5, 0.1), Layer(1.4, 0.3, 30.0, 0.8, 0.05), Layer.slide(1.5, 0.1)],
+            Spheres(R=True, R_pw=1.0, R_fs=0.002, R_fp=0.3, R_fd=0.01, R_angle=0.2,
+                    T=False, T_pw=0.9, T_fs=0.1, T_fp=0.1, T_fd=0.1, T_angle=0.0)),
     }
