@@ -70,8 +70,8 @@ def bench1_layers():
 #                        unequal walls and both angle thresholds
 #   sphere_extremes      a thin slab between slides under a lossless R sphere
 #                        (wall 1.0) with a 0.2 % sample port and a 30 %
-#                        entrance port; no T sphere, with a zero acceptance
-#                        angle
+#                        entrance port; no T sphere, with the reference's
+#                        0.22-degree acceptance angle
 def extreme_stacks():
     return {
         "anisotropy_extremes": (
@@ -87,5 +87,6 @@ def extreme_stacks():
         "sphere_extremes": (
             [Layer.slide(1.5, 0.1), Layer(1.4, 0.3, 30.0, 0.8, 0.05), Layer.slide(1.5, 0.1)],
             Spheres(R=True, R_pw=1.0, R_fs=0.002, R_fp=0.3, R_fd=0.01, R_angle=0.2,
-                    T=False, T_pw=0.9, T_fs=0.1, T_fp=0.1, T_fd=0.1, T_angle=0.0)),
+                    T=False, T_pw=0.9, T_fs=0.1, T_fp=0.1, T_fd=0.1,
+                    T_angle=0.22 * math.pi / 180)),
     }

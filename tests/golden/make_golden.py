@@ -122,6 +122,33 @@ CASES = {
     # tissue directly against ambient on both faces, both spheres, thicker slab
     "bare_two_layer": ("ISMLMC", [layer(1.4, 0.5, 50.0, 0.85, 0.1),
                                   layer(1.33, 0.2, 30.0, 0.7, 0.2)], spheres(), 400000, 64, 4000),
+    # anisotropy extremes: back-scattering, strongly forward, undeflected and
+    # isotropic layers, the first two index-matched to the ambient (n = 1)
+    "anisotropy_extremes": ("ISMLMC", [layer(1.0, 0.5, 40.0, -0.9, 0.1),
+                                       layer(1.0, 0.2, 60.0, 0.99, 0.1),
+                                       layer(1.33, 0.3, 30.0, 1.0, 0.05),
+                                       layer(1.33, 0.1, 20.0, 0.0, 0.05)], spheres(),
+                            2000000, 64, 4300),
+    # strong index contrast: n = 2.4 tissue 20 um thick under an n = 1.8 slide,
+    # a strong absorber, a highly scattering layer, an n = 1.45 slide; large
+    # ports, unequal walls, both angle thresholds
+    "index_contrast": ("ISMLMC", [layer(1.8, 0.0, 0.0, 0.0, 0.05),
+                                  layer(2.4, 0.2, 80.0, 0.85, 0.002),
+                                  layer(1.33, 30.0, 5.0, 0.5, 0.05),
+                                  layer(1.55, 0.05, 300.0, 0.95, 0.08),
+                                  layer(1.45, 0.0, 0.0, 0.0, 0.2)],
+                       dict(R=True, R_pw=0.995, R_fs=0.08, R_fp=0.06, R_fd=0.02,
+                            R_f=0.08 + 0.06 + 0.02, R_angle=0.3, specular_included=False,
+                            T=True, T_pw=0.9, T_fs=0.12, T_fp=0.01, T_fd=0.05,
+                            T_f=0.12 + 0.01 + 0.05, T_angle=0.01), 2000000, 64, 4400),
+    # sphere extremes: a lossless R sphere with a 0.2 % sample port and a 30 %
+    # entrance port; no T sphere, the reference's 0.22-degree acceptance angle
+    "sphere_extremes": ("ISMLMC", [GLASS15, layer(1.4, 0.3, 30.0, 0.8, 0.05), GLASS15],
+                        dict(R=True, R_pw=1.0, R_fs=0.002, R_fp=0.3, R_fd=0.01,
+                             R_f=0.002 + 0.3 + 0.01, R_angle=0.2, specular_included=False,
+                             T=False, T_pw=0.9, T_fs=0.1, T_fp=0.1, T_fd=0.1,
+                             T_f=0.1 + 0.1 + 0.1, T_angle=0.22 * math.pi / 180), 2000000, 64,
+                        4500),
 }
 
 
