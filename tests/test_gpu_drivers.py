@@ -155,3 +155,23 @@ def test_lookup_driver_cuda_path_gpu_tables(tmp_path):
     assert os.path.exists(tables + ".npz") or os.path.exists(tables + ".h5")
     # the table is 300 x 300 over 0-100 % in R and T: lookups resolve ~0.3 %
     _reproduces(cp, float(ma.group(1)), float(ms.group(1)), 0.08)
+
+
+@_need("Lookup/lookup.py")
+def test_lookup_driver_python_path_gpu_tables(tmp_path):
+    """lookup.py --Python with the GPU tables: the reference's own
+    sample_space loop (lookup.py:228-259) calls the drop-in ISMC for every
+    grid point, run and input sample; the GPU makelookup builds the tables,
+    and the driver's own lookup of the example measurement must fit it."""
+    edits = {**_EXACT, ("lookup", "N"): 50000, ("lookup", "runs"): 2,
+             ("lookup", "dimensions"): 300, ("lookup", "simulation_distributions_samples"): 20,
+             ("lookup", "measurement_distributions_samples"): 100,
+             ("lookup", "input_distributions_samples"): 2}
+    drv, ini, cp = _copy(tmp_path, "Lookup/lookup.py", edits)
+    out = _run(drv, ["--gpu-tables", "--numpy-seed", "5", "--ismc-seed", "7", "--Python", ini],
+               os.path.dirname(drv))
+    ma = re.search(r"mua = (\S+) \+/- (\S+) for R_d", out)
+    ms = re.search(r"mus' = (\S+) \+/- (\S+) for R_d", out)
+    assert ma and ms, out[-2000:]
+    assert out.count("RUN: ") == 13 * 11 * 2 * 2          # grid x runs x input samples
+    _reproduces(cp, float(ma.group(1)), float(ms.group(1)), 0.08)
