@@ -175,3 +175,23 @@ def test_lookup_driver_python_path_gpu_tables(tmp_path):
     assert ma and ms, out[-2000:]
     assert out.count("RUN: ") == 13 * 11 * 2 * 2          # grid x runs x input samples
     _reproduces(cp, float(ma.group(1)), float(ms.group(1)), 0.08)
+
+
+@_need("Lookup/lookup.py")
+def test_lookup_driver_python_path_reference_tables(tmp_path):
+    """lookup.py --Python without the GPU tables: the driver's own
+    makelookup (scipy griddata and its Python uncertainty loop,
+    lookup.py:301-465) turns the drop-in ISMC grid into the tables, at a
+    150 x 150 resolution to keep its loop short."""
+    edits = {**_EXACT, ("lookup", "N"): 50000, ("lookup", "runs"): 2,
+             ("lookup", "dimensions"): 150, ("lookup", "simulation_distributions_samples"): 20,
+             ("lookup", "measurement_distributions_samples"): 100,
+             ("lookup", "input_distributions_samples"): 2}
+    drv, ini, cp = _copy(tmp_path, "Lookup/lookup.py", edits)
+    out = _run(drv, ["--numpy-seed", "5", "--ismc-seed", "7", "--Python", ini],
+               os.path.dirname(drv))
+    ma = re.search(r"mua = (\S+) \+/- (\S+) for R_d", out)
+    ms = re.search(r"mus' = (\S+) \+/- (\S+) for R_d", out)
+    assert ma and ms, out[-2000:]
+    # a 150 x 150 table over 0-100 % in R and T resolves ~0.7 %
+    _reproduces(cp, float(ma.group(1)), float(ms.group(1)), 0.10)
