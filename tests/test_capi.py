@@ -81,3 +81,23 @@ def test_errors_without_gpu(lib):
     assert lib.ismc_init(0, None) == _abi.ERR_INVALID_ARG
     assert lib.ismc_run(None, None, None, 0, 0, 0, None) == _abi.ERR_INVALID_ARG
     assert lib.ismc_run_batch(None, None, 0, None, None) == _abi.ERR_INVALID_ARG
+
+
+def test_integration_cpp_shim_compiles(tmp_path):
+    """The C++ shim INTEGRATION.md gives the reference's CUDA callers (the
+    ISMLMC() signature of CUDA/CUDAISMLMC.h:656 over ismc_run) compiles
+    against include/ismc.h."""
+    import shutil
+    import subprocess
+    with open(os.path.join(ROOT, "INTEGRATION.md")) as fh:
+        blocks = re.findall(r"```cpp\n(.*?)```", fh.read(), re.S)
+    assert blocks
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    if shutil.which("g++") is None or not os.path.isdir(os.path.join(cuda_inc, "cccl")):
+        pytest.skip("g++ or the CUDA toolkit's thrust headers are absent")
+    src = tmp_path / "shim.cpp"
+    src.write_text(blocks[0])
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I" + os.path.join(ROOT, "include"),
+                        "-I" + cuda_inc, "-I" + os.path.join(cuda_inc, "cccl"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
