@@ -187,12 +187,13 @@ def cpu_baseline(seconds=12.0, stack="bench1"):
                       f"{threads} threads, {dt:.1f} s)", "steps_per_s": steps / dt}
 
 
-def cpu_solve_baseline(engine, seconds=60.0, packets=100_000):
+def cpu_solve_baseline(engine, seconds=150.0, packets=100_000, solves=10):
     """The reference's Python minimisation path (minimization.py:199-271:
     scipy Powell on the reference's cost, one N-packet forward run per
     objective) with the FP64 restatement of ISMLMC.py on all host cores as
-    the forward model, on a few of the solve benchmark's measurements, for
-    about `seconds`.  Reported beside the GPU paths."""
+    the forward model, on the first `solves` of the solve benchmark's
+    measurements, stopping early after about `seconds`.  Reported beside the
+    GPU paths."""
     import math
     import numpy as np
     from scipy.optimize import minimize
@@ -203,7 +204,7 @@ def cpu_solve_baseline(engine, seconds=60.0, packets=100_000):
     from ismc_gb300.workloads import bench_spheres
     threads = host_cores()
     sph = bench_spheres()
-    truth, meas = make_measurements(engine, 8, seed=4)
+    truth, meas = make_measurements(engine, solves, seed=4)
     evals = [0]
 
     def cost(x, m, k):
