@@ -149,6 +149,17 @@ CASES = {
                              T=False, T_pw=0.9, T_fs=0.1, T_fp=0.1, T_fd=0.1,
                              T_f=0.1 + 0.1 + 0.1, T_angle=0.22 * math.pi / 180), 2000000, 64,
                         4500),
+    # a non-absorbing thin layer between slides: no roulette, weight 1 to the end
+    "nonabsorbing_thin": ("ISMLMC", [GLASS15, layer(1.4, 0.0, 50.0, 0.9, 0.02), GLASS15],
+                          spheres(), 2000000, 64, 4600),
+    # single-slab driver with the 8-degree launch, T sphere only (R by angle)
+    "slab_specular_T_only": ("ISMC", [layer(1.33, 0.5, 20.0, 0.8, 0.2)],
+                             spheres(R=False, specular_included=True), 2000000, 64, 4700),
+    # three isotropic layers of different index, no slides, both spheres
+    "isotropic_stack": ("ISMLMC", [layer(1.3, 0.1, 10.0, 0.0, 0.1),
+                                   layer(1.5, 0.3, 25.0, 0.0, 0.05),
+                                   layer(1.4, 0.05, 15.0, 0.0, 0.15)], spheres(),
+                        2000000, 64, 4800),
 }
 
 
