@@ -65,3 +65,17 @@ def test_bench_refpython_arm_prints_its_line():
     assert line["config"]["packets_per_step"] >= 400
     assert line["e2e"]["h2d_bytes_per_step"] == 0
     assert abs(sum(line["result"]["mean"]) - 1.0) < 0.05
+
+
+def test_refpython_baseline_line():
+    """The GPU arm's cpu_baseline where the reference's Python is staged: a
+    bounded sample on every host core, kind "reference"."""
+    import os
+    import sys
+    _model()
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import bench
+    b = bench.refpython_baseline(seconds=0.2, stack="bench0")
+    assert b["kind"] == "reference" and b["value"] > 0
+    assert b["cores"] == bench.host_cores() and "ISMLMC.py" in b["sample"]
