@@ -10,6 +10,8 @@
   the photon budgets scaled by 1e-2 to keep the test short. For a seeded
   sample of instances, each instance's tallies from the batch equal those
   of the same instance run alone.
+* 5e9 packets of the multilayer stack in one call, above the per-instance
+  limit: run as consecutive packet ranges and merged exactly.
 """
 import numpy as np
 import pytest
@@ -64,3 +66,23 @@ def test_lookup_workload_full_instance_count(engine):
     for k in sample:
         alone = engine.run_batch_raw([insts[k]])[0]
         assert _same(batch[k], alone), k
+
+
+def test_instance_above_the_per_instance_limit(engine):
+    """5e9 packets of the multilayer benchmark stack in one Engine.run_batch
+    call: above ISMC_MAX_PACKETS (2^31), so the API runs three consecutive
+    packet ranges in one launch and adds their tallies as Python integers
+    (the A sum alone passes 2^63).  The merged means agree with the
+    reference's own runs within 3 combined standard errors, and their
+    standard errors are sqrt(50) times smaller than those of a 1e8 run."""
+    c = cases.golden()["bench1_multilayer"]
+    N = 5_000_000_000
+    inst = cases.case_instance(c, N, seed=77)
+    r = engine.run_batch([inst])[0]
+    assert r.status == 0 and r.n == N
+    assert r.sums[0] > 2 ** 63
+    z = cases.zscores(r.mean, r.se, c["mean"], c["se"])
+    assert max(abs(x) for x in z) <= 3.0, z
+    small = engine.run_batch([cases.case_instance(c, 100_000_000, seed=77)])[0]
+    for k in (1, 3):
+        assert abs(small.se[k] / r.se[k] / np.sqrt(50) - 1) < 0.05
