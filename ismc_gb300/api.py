@@ -13,7 +13,7 @@ import math
 import os
 import threading
 from dataclasses import dataclass, field
-from typing import Iterable, List, Optional, Sequence
+from typing import List, Optional, Sequence
 
 from . import _abi
 

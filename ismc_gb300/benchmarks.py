@@ -48,7 +48,7 @@ def run_tables(engine, grid=64, N=1000, M=100, packets=100_000, runs=4, seed=3):
     launch, then the four Clough-Tocher tables and the Monte Carlo uncertainty
     map on the GPU.  Returns timings and the inputs (for a CPU comparison)."""
     from .api import Layer
-    from .lookup import interp_table, make_lookup, sample_space
+    from .lookup import make_lookup, sample_space
     mu_a = np.logspace(np.log10(0.01), np.log10(10.0), grid)
     mus_r = np.logspace(0.0, 2.0, grid)
     sl = (Layer.slide(1.5, 0.1), Layer.slide(1.5, 0.1))

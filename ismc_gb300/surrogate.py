@@ -22,8 +22,7 @@ import time
 
 import numpy as np
 
-from . import _abi
-from .api import (Engine, IsmcError, Layer, load_library, make_solve, slab_instances,
+from .api import (IsmcError, Layer, load_library, make_solve, slab_instances,
                   tallies_mean_se)
 from .workloads import bench_spheres
 

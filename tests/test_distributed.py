@@ -5,7 +5,6 @@ a single-process run over the whole range bit for bit."""
 import os
 import socket
 
-import pytest
 import torch.multiprocessing as mp
 
 

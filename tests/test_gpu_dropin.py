@@ -1,6 +1,5 @@
 """The drop-in modules keep the reference's call surface (ISMC.py:164-165,
 ISMLMC.py:101-102) and statistics."""
-import math
 
 import pytest
 

@@ -2,7 +2,6 @@
 FP64 product of the same BF16 operands, the MLP gradients against the FP64
 numpy oracle (oracle/mlp64.py, with BF16 rounding at the same storage points),
 and that training on the GPU lowers the loss."""
-import ctypes as C
 
 import numpy as np
 import pytest

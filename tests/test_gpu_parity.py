@@ -14,7 +14,6 @@
    a bit of the result.
 """
 import ctypes as C
-import math
 
 import numpy as np
 import pytest
@@ -22,7 +21,7 @@ import pytest
 import cases
 import oracle
 from conftest import PARITY_Z
-from ismc_gb300 import Layer, Spheres, _abi, make_instance, make_tune, tally_to_result
+from ismc_gb300 import Layer, Spheres, _abi, make_instance, make_tune
 
 pytestmark = pytest.mark.gpu
 

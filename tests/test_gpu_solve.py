@@ -1,7 +1,6 @@
 """Batched plain-path inverse solve on the GPU (PRAXIS + Monte Carlo
 objective, minimization.py:201-271): recovers known optical properties, and
 every round of objective evaluations is one batched launch."""
-import math
 
 import pytest
 
