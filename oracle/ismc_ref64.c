@@ -9,6 +9,8 @@
  *   ref_reincidence ........ ISMC.py:80-81
  *   ref_mc_single .......... ISMC.py:87-160  (slab walk, mirror boundaries)
  *   ref_mc_multi ........... MLMC.py:76-202  (multilayer step-to-boundary walk)
+ *   ref_mc_multi_physical .. the same walk in the kernel's physical mode (no
+ *                            counterpart in the reference)
  *   ref_driver ............. ISMC.py:164-406 / ISMLMC.py:101-347
  *
  * Random numbers: the reference draws Python `random.uniform(0,1)` (Mersenne
@@ -94,6 +96,30 @@ typedef struct {
 typedef struct { double absorbed, reflected, transmitted, ux, uy, uz; uint64_t steps; } Walk;
 
 /* ISMC.py:87-160 */
+/* Henyey-Greenstein deflection and azimuth, and the direction rotation with
+ * its normal-incidence branch (MLMC.py:187-200) */
+static void ref_spin(double gg, Rng* g, double* ux, double* uy, double* uz) {
+    double ct;
+    if (gg == 0.0) ct = 2 * uniform(g) - 1;
+    else {
+        const double q = (1 - gg * gg) / (1 - gg + 2 * gg * uniform(g));
+        ct = (1 / (2 * gg)) * (1 + gg * gg - q * q);
+    }
+    const double phi = 2 * M_PI * uniform(g);
+    const double cp = cos(phi), sp = sin(phi);
+    const double st = sqrt(1.0 - ct * ct);
+    double nx, ny, nz;
+    if (fabs(*uz) > 0.99999) {
+        nx = st * cp; ny = st * sp; nz = (*uz / fabs(*uz)) * ct;
+    } else {
+        const double zs = sqrt(1 - *uz * *uz);
+        nx = st / zs * (*ux * *uz * cp - *uy * sp) + *ux * ct;
+        ny = st / zs * (*uy * *uz * cp + *ux * sp) + *uy * ct;
+        nz = -1.0 * st * cp * zs + *uz * ct;
+    }
+    *ux = nx; *uy = ny; *uz = nz;
+}
+
 static void ref_mc_single(const Stack* S, double w, double z, double ux, double uy, double uz,
                           Rng* g, Walk* o) {
     const double n = S->n[0], mua = S->mua[0], mut = S->mut[0], gg = S->g[0], t = S->t[0];
@@ -193,27 +219,69 @@ static void ref_mc_multi(const Stack* S, double w, double z, double ux, double u
             A += dW;
         }
         if (w <= threshold) w = (uniform(g) <= 1.0 / m) ? m * w : 0;
-        if (w > 0 && S->mus[layer] != 0) {
-            const double gg = S->g[layer];
-            double ct;
-            if (gg == 0.0) ct = 2 * uniform(g) - 1;
-            else {
-                const double q = (1 - gg * gg) / (1 - gg + 2 * gg * uniform(g));
-                ct = (1 / (2 * gg)) * (1 + gg * gg - q * q);
+        if (w > 0 && S->mus[layer] != 0) ref_spin(S->g[layer], g, &ux, &uy, &uz);
+    }
+    o->absorbed = A; o->reflected = Rf; o->transmitted = Tr; o->ux = ux; o->uy = uy; o->uz = uz;
+}
+
+/*
+ * Physical mode (no counterpart in the reference; the kernel's mode
+ * ISMC_MODE_PHYSICAL).  Same step-to-boundary walk, except that
+ *   - the free path is carried as optical depth tau, so what is left when a
+ *     packet leaves a scattering layer survives a slide and is spent in the
+ *     next scattering layer (the compat walk restarts with s = 0 there);
+ *   - a slide absorbs by Beer-Lambert, w *= exp(-mua d), over the path d
+ *     inside it (the compat walk ignores slide mua);
+ *   - the first tau is drawn by the caller at incidence, even under a slide.
+ */
+static void ref_mc_multi_physical(const Stack* S, double w, double z, double ux, double uy,
+                                  double uz, double tau, Rng* g, double threshold, double m,
+                                  Walk* o) {
+    double A = 0, Rf = 0, Tr = 0;
+    int layer = uz > 0 ? 0 : S->L - 1;
+    uint64_t events = 0;
+    o->steps = 0;
+    while (w > 0) {
+        if (++events > 100000000ull) { w = 0; break; }
+        double d;
+        int next;
+        if (uz < 0) { d = (S->bounds[layer] - z) / uz; next = layer - 1; }
+        else if (uz > 0) { d = (S->bounds[layer + 1] - z) / uz; next = layer + 1; }
+        else { d = INFINITY; next = layer; }
+        if (S->mus[layer] == 0) {
+            if (!(d < INFINITY)) { w = 0; break; }        /* a slide cannot be left */
+            const double wn = w * exp(-S->mua[layer] * d);
+            A += w - wn;
+            w = wn;
+        } else {
+            const double s = tau / S->mut[layer];
+            if (s < d) {
+                /* hop, drop, roulette, spin, next free path (MLMC.py:165-200) */
+                z += s * uz;
+                ++o->steps;
+                const double dW = w * S->mua[layer] / S->mut[layer];
+                w -= dW;
+                A += dW;
+                if (w <= threshold) w = (uniform(g) <= 1.0 / m) ? m * w : 0;
+                if (w > 0) {
+                    ref_spin(S->g[layer], g, &ux, &uy, &uz);
+                    double u = uniform(g);
+                    if (u <= 0) u = 1e-300;
+                    tau = -log(u);
+                }
+                continue;
             }
-            const double phi = 2 * M_PI * uniform(g);
-            const double cp = cos(phi), sp = sin(phi);
-            const double st = sqrt(1.0 - ct * ct);
-            double nx, ny, nz;
-            if (fabs(uz) > 0.99999) {
-                nx = st * cp; ny = st * sp; nz = (uz / fabs(uz)) * ct;
-            } else {
-                const double zs = sqrt(1 - uz * uz);
-                nx = st / zs * (ux * uz * cp - uy * sp) + ux * ct;
-                ny = st / zs * (uy * uz * cp + ux * sp) + uy * ct;
-                nz = -1.0 * st * cp * zs + uz * ct;
-            }
-            ux = nx; uy = ny; uz = nz;
+            tau -= d * S->mut[layer];
+        }
+        z = uz > 0 ? S->bounds[layer + 1] : S->bounds[layer];
+        const double nn = (next == S->L || next == -1) ? 1.0 : S->n[next];
+        if (uniform(g) < ref_fresnel_snell(S->n[layer], nn, uz)) {
+            uz *= -1;
+        } else {
+            ref_snell(S->n[layer], nn, &ux, &uy, &uz);
+            if (next == S->L) { Tr += w; w = 0; break; }
+            if (next == -1) { Rf += w; w = 0; break; }
+            layer = next;
         }
     }
     o->absorbed = A; o->reflected = Rf; o->transmitted = Tr; o->ux = ux; o->uy = uy; o->uz = uz;
@@ -221,6 +289,7 @@ static void ref_mc_multi(const Stack* S, double w, double z, double ux, double u
 
 typedef struct {
     int single;     /* 1: ISMC.py driver (one slab), 0: ISMLMC.py driver */
+    int physical;   /* ISMC_MODE_PHYSICAL (stack driver only) */
     Stack S;
     ismc_spheres P;
     double threshold, m;
@@ -239,7 +308,8 @@ static int ref_sphere(const Setup* st, int side, double w, double* ux, double* u
         const double pw = side ? P->T_pw : P->R_pw, fs = side ? P->T_fs : P->R_fs,
                      f = side ? P->T_f : P->R_f;
         if (uniform(g) < (pw * fs) / (1 - pw * (1 - f))) {
-            const double mz = uniform(g);
+            /* mu_z ~ U (ISMC.py:207); cosine-weighted sqrt(U) in physical mode */
+            const double mz = st->physical ? sqrt(uniform(g)) : uniform(g);
             const double phi = 2 * M_PI * uniform(g);
             *uz = side ? -1 * mz : mz;
             *ux = cos(phi) * sqrt(1 - (*uz) * (*uz));
@@ -270,6 +340,10 @@ static void ref_packet(const Setup* st, Rng* g, double x[5], uint64_t* steps) {
         int reflect;
         if (st->single) {
             reflect = !(uniform(g) > ref_fresnel_snell(1.0, S->n[0], uz));
+        } else if (st->physical) {
+            /* one Fresnel draw at the outer face; a slide's inner face is
+             * met by the walk */
+            reflect = uniform(g) < ref_fresnel_snell(1.0, S->n[layer], uz);
         } else if (S->mus[layer] == 0.0) {
             const double n1 = 1.0, n2 = S->n[layer];
             const double n3 = uz > 0 ? (layer + 1 < S->L ? S->n[layer + 1] : 1.0)
@@ -288,8 +362,15 @@ static void ref_packet(const Setup* st, Rng* g, double x[5], uint64_t* steps) {
         }
         ref_snell(1.0, S->n[layer], &ux, &uy, &uz);
         Walk o;
-        if (st->single) ref_mc_single(S, w, z, ux, uy, uz, g, &o);
-        else ref_mc_multi(S, w, z, ux, uy, uz, g, st->threshold, st->m, &o);
+        if (st->single) {
+            ref_mc_single(S, w, z, ux, uy, uz, g, &o);
+        } else if (st->physical) {
+            double u = uniform(g);
+            if (u <= 0) u = 1e-300;
+            ref_mc_multi_physical(S, w, z, ux, uy, uz, -log(u), g, st->threshold, st->m, &o);
+        } else {
+            ref_mc_multi(S, w, z, ux, uy, uz, g, st->threshold, st->m, &o);
+        }
         *steps += o.steps;
         x[ISMC_T_A] += o.absorbed;
         ux = o.ux; uy = o.uy; uz = o.uz;
@@ -340,6 +421,7 @@ int ref64_run(int single, const ismc_instance* inst, int threads, double sum[5],
     Setup st;
     memset(&st, 0, sizeof st);
     st.single = single;
+    st.physical = !single && inst->mode == ISMC_MODE_PHYSICAL;
     st.S.L = (int)inst->stack.L;
     st.S.bounds[0] = 0;
     for (int l = 0; l < st.S.L; ++l) {

@@ -90,3 +90,21 @@ def extreme_stacks():
                     T=False, T_pw=0.9, T_fs=0.1, T_fp=0.1, T_fd=0.1,
                     T_angle=0.22 * math.pi / 180)),
     }
+
+
+# Stacks for the physical mode (no counterpart in the reference), checked
+# against the FP64 physical walk of oracle/ismc_ref64.c:
+#   bench1                   the multilayer benchmark stack
+#   absorbing_slides         slides that absorb (mua 0.8 and 2.0: Beer-Lambert)
+#                            around the single-layer slab
+#   index_contrast           the extreme index-contrast stack above
+#   slab_slides_T_only       the single-layer configuration, T sphere only
+def physical_stacks():
+    return {
+        "bench1": (bench1_layers(), bench_spheres()),
+        "absorbing_slides": ([Layer(1.5, 0.8, 0.0, 0.0, 0.1), Layer(1.4, 1.0, 100.0, 0.9, 0.1),
+                              Layer(1.45, 2.0, 0.0, 0.0, 0.15)], bench_spheres()),
+        "index_contrast": extreme_stacks()["index_contrast"],
+        "slab_slides_T_only": (bench0_layers(),
+                               Spheres.from_radii(5.08, 1.27, 1.27, 0.635, 0.98, R=False, T=True)),
+    }

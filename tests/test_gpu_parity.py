@@ -170,6 +170,19 @@ def test_gpu_extreme_stacks_match_fp64_restatement(engine, name):
     assert r.status == 0 and max(abs(x) for x in z) <= 3.0, (z, r.mean, m)
 
 
+@pytest.mark.parametrize("name", sorted(cases.physical_stacks()))
+def test_gpu_physical_mode_matches_fp64_physical_walk(engine, name):
+    """The physical mode on the GPU (2e6 packets) against the independent
+    FP64 physical walk of oracle/ismc_ref64.c (1e6 packets), 3 combined
+    standard errors per tally (tests/cases.py physical_stacks: the benchmark
+    stack, absorbing slides, strong index contrast, T sphere only)."""
+    layers, sph = cases.physical_stacks()[name]
+    r = engine.run_batch([make_instance(layers, sph, 2_000_000, seed=22, mode="physical")])[0]
+    m, se, _ = oracle.ref64_run(make_instance(layers, sph, 1_000_000, seed=23, mode="physical"))
+    z = cases.zscores(r.mean, r.se, m, se)
+    assert r.status == 0 and max(abs(x) for x in z) <= 3.0, (z, r.mean, m)
+
+
 def test_gpu_physical_equals_compat_without_slides_or_spheres(engine):
     """With no slide and no sphere the two modes take identical decisions."""
     sp = Spheres(R=False, T=False)

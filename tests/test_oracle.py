@@ -73,6 +73,23 @@ def test_twin_vs_ref64_extreme_stacks(name):
     assert max(abs(x) for x in z) <= 3.0, z
 
 
+@pytest.mark.parametrize("name", sorted(cases.physical_stacks()))
+def test_twin_vs_ref64_physical_mode(name):
+    """The physical mode (optical depth kept across slides, Beer-Lambert in
+    slides, one Fresnel draw at incidence, cosine-weighted re-incidence) of
+    the FP32 twin against the independent FP64 physical walk of
+    oracle/ismc_ref64.c, 3 combined standard errors per tally.  The GPU draws
+    the twin's tallies bit for bit."""
+    from ismc_gb300 import make_instance
+    layers, sph = cases.physical_stacks()[name]
+    r = tally_to_result(oracle.twin_run(make_instance(layers, sph, 2_000_000, seed=22,
+                                                      mode="physical")))
+    mean, se, _ = oracle.ref64_run(make_instance(layers, sph, 1_000_000, seed=23,
+                                                 mode="physical"))
+    z = cases.zscores(r.mean, r.se, mean, se)
+    assert max(abs(x) for x in z) <= 3.0, z
+
+
 def test_twin_thread_invariance():
     """Integer tallies do not depend on how packets are split across threads."""
     c = cases.golden()["five_layer_mixed"]
