@@ -8,7 +8,11 @@ Contents
   twin_run      FP32 C restatement of the GPU event algorithm, same Philox
                 streams: must equal the GPU's integer tallies bit for bit.
   ref64_run     FP64 C restatement of the reference's ISMC.py / ISMLMC.py
-                structure (statistical oracle and CPU baseline).
+                structure (statistical oracle and CPU baseline), with an FP64
+                walk of the kernel's physical mode for instances in that mode.
+  build_ref / refpython  the reference's own sources staged into oracle/_ref/
+                (PRAXIS, the CUDA model, the drivers, the Python model) and a
+                process pool that runs the staged ISMLMC.py.
   analytic64    FP64 specular / ballistic values of a stack (oracle/analytic64.py).
   golden_cases  statistical fixtures produced by the reference's own Python
                 (tests/golden/reference_cases.json, made by tests/golden/make_golden.py).
