@@ -160,3 +160,30 @@ def test_merge_tallies_adds_exactly_beyond_64_bits():
         t.sumsq[0] = 2 ** 63
     r = merge_tallies(big)
     assert r.sums[0] == 3 * 2 ** 63 and r.mean[0] == 1.0 and r.se[0] == 0.0
+
+
+def test_bench_clock_sampler_against_a_fake_nvidia_smi(tmp_path, monkeypatch):
+    """bench.py's clock record: median SM clock under load, the maximum, and
+    the throttle reasons that were active, from nvidia-smi's CSV rows (a
+    stand-in script here); entering the sampler waits for its first row."""
+    import os
+    import stat
+    import sys
+    fake = tmp_path / "nvidia-smi"
+    rows = ["0, 2070, 2070, 800.5, 0x0, Not Active, Not Active, Not Active, Not Active",
+            "0, 2070, 2070, 900.1, 0x4, Not Active, Not Active, Not Active, Active",
+            "0, 1965, 2070, 1000.0, 0x4, Not Active, Not Active, Not Active, Active"]
+    fake.write_text("#!/bin/sh\nsleep 0.3\n" + "".join(f"echo '{r}'\n" for r in rows) +
+                    "sleep 5\n")
+    fake.chmod(fake.stat().st_mode | stat.S_IEXEC)
+    monkeypatch.setenv("PATH", str(tmp_path) + os.pathsep + os.environ["PATH"])
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import bench
+    with bench.ClockSampler(0) as clk:
+        assert clk.rows                      # the first sample is in before timing starts
+        import time
+        time.sleep(0.3)
+    s = clk.summary()
+    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"] and s["samples"] == 3
