@@ -119,9 +119,9 @@ def run_surrogate(engine, n_samples=1 << 20, packets=100_000, epochs=20, batch=4
     return sur, out
 
 
-def run_solve(engine, sur, n_meas=10000, n_plain=200, seed=4, verify_packets=1_000_000,
+def run_solve(engine, sur, n_meas=10000, n_plain=200, seed=4, verify_packets=300_000,
               plain_packets=100_000, conv_packets=1_000_000, n_conv_repeat=100,
-              anchor_packets=300_000, ref_anchor_packets=200_000):
+              anchor_packets=300_000, ref_anchor_packets=200_000, ref_verify_packets=1_000_000):
     """Inverse solves of the benchmark's synthetic measurements, four ways.
 
     plain       PRAXIS on the reference's cost with `plain_packets` per
@@ -140,8 +140,10 @@ def run_solve(engine, sur, n_meas=10000, n_plain=200, seed=4, verify_packets=1_0
                 and verified with `verify_packets` under the goodness-of-fit
                 test.
     reference   the same path minimising the plain path's own cost, anchored
-                with `ref_anchor_packets`, under the surrogate-vs-Monte Carlo
-                test."""
+                with `ref_anchor_packets` and verified with
+                `ref_verify_packets`, under the surrogate-vs-Monte Carlo test
+                (whose tolerance grows with the verifying run's standard
+                error, so it keeps the larger run)."""
     from .surrogate import sample_stack, surrogate_solve
     truth, meas = make_measurements(engine, n_meas, seed=seed)
     sig = np.array([0.002, 0.002, 0.0005])
@@ -186,7 +188,7 @@ def run_solve(engine, sur, n_meas=10000, n_plain=200, seed=4, verify_packets=1_0
     xs = rs["x"]
     # the same path on the plain path's own cost
     t2 = time.perf_counter()
-    r2 = surrogate_solve(sur, engine, meas, sig, verify_packets=verify_packets,
+    r2 = surrogate_solve(sur, engine, meas, sig, verify_packets=ref_verify_packets,
                          plain_packets=plain_packets, seed=seed + 99, objective="reference",
                          anchor_packets=ref_anchor_packets)
     t_ref = time.perf_counter() - t2
@@ -199,7 +201,8 @@ def run_solve(engine, sur, n_meas=10000, n_plain=200, seed=4, verify_packets=1_0
     return {"measurements": n_meas, "plain_subsample": k, "converged_repeat": kr,
             "objective": "chi2",
             "packets": {"plain": plain_packets, "converged": conv_packets,
-                        "anchor": anchor_packets, "verify": verify_packets},
+                        "anchor": anchor_packets, "verify": verify_packets,
+                        "reference_objective_verify": ref_verify_packets},
             "plain_solves_per_s": k / t_plain, "plain_evals_mean": float(ev.mean()),
             "converged_solves_per_s": k / t_conv, "converged_evals_mean": float(evc.mean()),
             "surrogate_solves_per_s": n_meas / t_sur,
